@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Benchmark of the tortuosity engine on one GB300 (or N replicas).
+
+Workload (one "step"): the 256^3 packed-ellipsoid volume (seed 1, semi-major
+axis 12 voxels, aspect 0.35, solid fraction 0.55; pore D = 1, solid D = 1e-3,
+arithmetic face mean), tau in the three directions x, y, z solved as three
+right-hand sides sharing one phase field, BiCGSTAB, FP32 inner iterations with
+FP64 iterative refinement, tolerance 1e-6 on the FP64 relative residual.
+Metric: tau solves/s (3 per step).  Inputs are synthetic: the reference's
+packer cannot run here, so the engine's seeded generator makes a volume of
+the same size, shape parameters and solid fraction.
+
+  value   device-resident mask, CUDA events on the launching stream around
+          exactly K steps, max over ranks.
+  e2e     the public C ABI with a HOST mask (fast_tau_solve_dirs): host to
+          device copy of the mask and device to host copy of the results
+          inside the timed region.
+  roofline the dominant kernel's algorithmic bytes per launch / its average
+          CUDA-event duration from one profiled step of the same workload.
+  cpu_baseline  the CPU oracle (a C/OpenMP restatement of the reference's
+          --cpu path: stored 7-coefficient system + Eigen-style BiCGSTAB, FP64)
+          timed on a bounded sample of the same volume and direction.
+
+``--impl reference`` times that CPU restatement alone (the reference itself
+cannot be built here: Eigen and glm are absent) and prints its JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = dict(name="ellipsoids256_xyz_bicgstab_mixed", shape=(256, 256, 256), seed=1, semi_major=12.0,
+                aspect=0.35, solid_fraction=0.55, dirs=(0, 2, 4), tol=1e-6, max_iter=10000)
+
+# Compulsory bytes per voxel of each kernel of the FP32-inner BiCGSTAB step
+# (each stream the kernel touches read or written once; neighbour re-reads
+# served on chip).  Step 1 reads r, p, v, r0, code and writes p, v; step 2
+# reads r, v, code; step 3 reads r, v, p, x, r0, code and writes x, r.
+KERNEL_BYTES_PER_VOXEL = {"bi1": 25, "bi2": 9, "bi3": 29, "bi_restart": 13, "refine": 37, "tau": 9,
+                          "init64": 12, "code": 2, "cg1": 13, "cg2": 21}
+# Algorithmic bytes per voxel-iteration of a whole FP32 BiCGSTAB iteration:
+# x, r, p, v read+written (32), r0 read (4), phase read twice (2).
+ITER_BYTES_FP32_BICGSTAB = 38
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_golden():
+    p = os.path.join(ROOT, "tests", "golden", "workloads.json")
+    try:
+        with open(p) as f:
+            return json.load(f)["workloads"].get("ellipsoids256")
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        first = vis.split(",")[0].strip() if vis else ""
+        self.index = int(first) if first.isdigit() else index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v: float, ws: int) -> float:
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_volume():
+    from fast_gb300 import volumes
+    w = WORKLOAD
+    return volumes.ellipsoids(w["shape"], w["seed"], w["semi_major"], w["aspect"], w["solid_fraction"])
+
+
+def cpu_sample(mask, dir_: int, full_iters: int, threads: int):
+    """Times the CPU oracle (stored system + BiCGSTAB, FP64) on this volume:
+    two bounded runs (5 and 25 iterations) give the setup and per-iteration
+    cost; a full solve is extrapolated to `full_iters` iterations."""
+    from oracle import oracle as O
+    O.build()
+    t = {}
+    for n in (5, 25):
+        t0 = time.perf_counter()
+        O.get_tortuosity(mask, dir=dir_, solver=O.BICGSTAB, tol=1e-6, max_iter=n, variant=O.EIGEN)
+        t[n] = time.perf_counter() - t0
+    per_iter = max((t[25] - t[5]) / 20.0, 1e-9)
+    setup = max(t[5] - 5 * per_iter, 0.0)
+    est = setup + full_iters * per_iter
+    return est, setup, per_iter, t[5] + t[25]
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the CPU restatement of the reference's path."""
+    if rank != 0:
+        return
+    mask = make_volume()
+    g = load_golden()
+    full = int(g["dirs"]["0"]["iters_bicgstab_1e-6"]) if g else 1000
+    threads = os.cpu_count() or 1
+    per_step = []
+    for i in range(args.warmup + args.steps):
+        est, setup, per_iter, wall = cpu_sample(mask, 0, full, threads)
+        if i >= args.warmup:
+            per_step.append(est)
+    t = statistics.mean(per_step)
+    value = 1.0 / t
+    line = {
+        "metric": "tau solves/s", "value": value, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD["name"], "volume": "256^3 ellipsoids seed 1 a=12 aspect 0.35 solid 0.55",
+                   "solver": "BiCGSTAB (Eigen recurrence, Jacobi)", "dirs": "x (one solve per step)",
+                   "tol": WORKLOAD["tol"]},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"oracle FP64 BiCGSTAB on the 256^3 volume, direction x: assembly + 5 and + 25 "
+                                   f"iterations timed, extrapolated to the {full} iterations of a full tol-1e-6 solve"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    import fast_gb300 as ft
+    from fast_gb300 import _native
+
+    w = WORKLOAD
+    mask = make_volume()
+    N = mask.size
+    dirs = [ft.Dir(d) for d in w["dirs"]]
+    params = ft.TortuosityParams(tolerance=w["tol"], max_iter=w["max_iter"], precision=ft.Precision.MIXED)
+    d_mask = torch.from_numpy(mask).cuda()
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def step():
+        return ft.solve_directions_device(d_mask.data_ptr(), mask.shape, dirs, params, ft.DSOLVER_BICGSTAB,
+                                          stream=sptr)
+
+    for _ in range(args.warmup):
+        res = step()
+    torch.cuda.synchronize()
+    ok = all(r.status == ft.Status.OK for r in res)
+
+    # --- timed region: exactly K steps, device-resident inputs
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    iters = []
+    launches = 0
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            res = step()
+            launches += _native.last_stats()["launches"]
+            iters.append(sum(r.iterations for r in res))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    ms_max = max_over_ranks(ms, ws)
+    solves = len(dirs) * args.steps * ws
+    value = solves / (ms_max / 1e3)
+
+    # --- end to end through the public C ABI with a host mask
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res_e2e = ft.solve_directions(mask, dirs, params, ft.DSOLVER_BICGSTAB)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
+    e2e_value = solves / e2e_s
+
+    # --- one profiled step: per-kernel CUDA-event durations
+    pparams = ft.TortuosityParams(tolerance=w["tol"], max_iter=w["max_iter"], precision=ft.Precision.MIXED,
+                                  profile=True)
+    pres = ft.solve_directions_device(d_mask.data_ptr(), mask.shape, dirs, pparams, ft.DSOLVER_BICGSTAB,
+                                      stream=sptr)
+    prof = _native.last_stats()
+    torch.cuda.synchronize()
+
+    if rank != 0:
+        return
+    peak, peak_kind = load_peaks()
+    total_inner = sum(r.iterations for r in pres)
+    kern = prof["kernels"]
+    # voxels processed by all launches of a kernel kind
+    vox = {"bi1": N * total_inner, "bi2": N * total_inner, "bi3": N * total_inner,
+           "refine": N * sum(r.outer_steps + 1 for r in pres), "tau": N * len(dirs), "code": N,
+           "init64": N * len(dirs)}
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    dom_bytes = KERNEL_BYTES_PER_VOXEL.get(dom, 0) * vox.get(dom, 0)
+    dom_ms = kern[dom]["ms"]
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    iter_ms = sum(kern.get(k, {"ms": 0})["ms"] for k in ("bi_restart", "bi1", "bi2", "bi3"))
+    iter_gbs = ITER_BYTES_FP32_BICGSTAB * N * total_inner / (iter_ms / 1e3) / 1e9 if iter_ms > 0 else 0.0
+    launches_per_step = launches / max(args.steps, 1)
+
+    # accuracy against the FP64 tol-1e-10 oracle
+    g = load_golden()
+    dtau = None
+    if g:
+        dtau = {}
+        for r in res:
+            ref = g["dirs"][str(int(r.dir))]["tau_cg_1e-10"]
+            dtau[r.dir.name] = abs(r.tau - ref) / ref
+
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        full = int(g["dirs"]["0"]["iters_bicgstab_1e-6"]) if g else 1000
+        threads = os.cpu_count() or 1
+        est, setup, per_iter, wall = cpu_sample(mask, 0, full, threads)
+        cpu = {"value": 1.0 / est, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": f"oracle FP64 BiCGSTAB (Eigen recurrence) on this volume, direction x: setup + 5 and + 25 "
+                         f"iterations timed ({wall:.1f} s), extrapolated to the {full} iterations of a full "
+                         f"tol-1e-6 solve: {setup:.2f} s + {per_iter * 1e3:.1f} ms/iter"}
+
+    line = {
+        "metric": "tau solves/s", "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded ellipsoid packing stand-in)",
+        "config": {"workload": w["name"], "volume": "256^3 ellipsoids seed 1 a=12 aspect 0.35 solid 0.55",
+                   "solver": "BiCGSTAB, Jacobi", "dirs": "x,y,z as 3 RHS", "precision": "FP32 inner + FP64 refinement",
+                   "tol": w["tol"], "parallelism": f"replicas x{ws}",
+                   "l2": "working set ~2.4 GB per step > 129 MB L2; no flush"},
+        "voxel_iters_per_s": N * (sum(iters) / len(iters)) * ws / (ms_max / 1e3 / args.steps),
+        "iterations_per_step": sum(iters) / len(iters),
+        "all_converged": ok,
+        "dtau_rel_vs_fp64_oracle": dtau,
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(N),
+                "d2h_bytes_per_step": int(len(dirs) * C_RESULT_BYTES)},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": dom_bytes / max(kern[dom]["launches"], 1),
+                     "avg_launch_ms": dom_ms / max(kern[dom]["launches"], 1),
+                     "traffic": NCU_TRAFFIC.get(dom),
+                     "iteration_gbs_at_38B": iter_gbs, "iteration_frac_at_38B": iter_gbs / peak},
+        "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in kern.items()},
+        "gpu_launches": int(launches),
+        "gpu_launches_per_step": launches_per_step,
+        "clocks": clk.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+C_RESULT_BYTES = 40  # sizeof(fast_tau_result)
+# DRAM bytes per launch of the dominant kernel from one ncu capture
+# (profiles/), null until captured.
+NCU_TRAFFIC = {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        from fast_gb300 import build
+        build.build()
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,65 @@
+// FP32 solver kernels: the reference's `-p float` (float scalars) and the
+// inner iterations of the MIXED solve (double scalars).
+#include "tau_launch.h"
+#include "tau_sweep.cuh"
+
+namespace ft {
+
+constexpr int kStages = 4;
+
+template <class Op>
+static void go(const Launch &L, cudaStream_t st)
+{
+    constexpr int dyn = sweep_dyn_smem<Op, kStages>();
+    sweep_kernel<Op, kStages><<<(unsigned)L.nblocks, NTHREADS, dyn, st>>>(L);
+}
+
+template <class Op>
+static cudaError_t cfg()
+{
+    return cudaFuncSetAttribute(sweep_kernel<Op, kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                sweep_dyn_smem<Op, kStages>());
+}
+
+template <typename ST>
+static void dispatch(Step s, const Launch &L, cudaStream_t st)
+{
+    using T = float;
+    switch (s) {
+    case Step::INIT_CG: go<OpInit<T, ST, false>>(L, st); break;
+    case Step::INIT_BI: go<OpInit<T, ST, true>>(L, st); break;
+    case Step::CG1: go<OpCG1<T, ST>>(L, st); break;
+    case Step::CG2: go<OpCG2<T, ST>>(L, st); break;
+    case Step::BI_RESTART: go<OpBiRestart<T, ST>>(L, st); break;
+    case Step::BI1: go<OpBi1<T, ST>>(L, st); break;
+    case Step::BI2: go<OpBi2<T, ST>>(L, st); break;
+    case Step::BI3: go<OpBi3<T, ST>>(L, st); break;
+    }
+}
+
+template <typename ST>
+static cudaError_t configure()
+{
+    using T = float;
+    cudaError_t e = cudaSuccess, r;
+    if ((r = cfg<OpInit<T, ST, false>>()) != cudaSuccess) e = r;
+    if ((r = cfg<OpInit<T, ST, true>>()) != cudaSuccess) e = r;
+    if ((r = cfg<OpCG1<T, ST>>()) != cudaSuccess) e = r;
+    if ((r = cfg<OpCG2<T, ST>>()) != cudaSuccess) e = r;
+    if ((r = cfg<OpBiRestart<T, ST>>()) != cudaSuccess) e = r;
+    if ((r = cfg<OpBi1<T, ST>>()) != cudaSuccess) e = r;
+    if ((r = cfg<OpBi2<T, ST>>()) != cudaSuccess) e = r;
+    if ((r = cfg<OpBi3<T, ST>>()) != cudaSuccess) e = r;
+    return e;
+}
+
+cudaError_t configure_f32()
+{
+    cudaError_t a = configure<float>(), b = configure<double>();
+    return a != cudaSuccess ? a : b;
+}
+
+void launch_pure_f32(Step s, const Launch &L, cudaStream_t st) { dispatch<float>(s, L, st); }
+void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st) { dispatch<double>(s, L, st); }
+
+}  // namespace ft

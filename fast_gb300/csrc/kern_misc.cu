@@ -1,0 +1,40 @@
+// Refinement, tau, stencil-code and initialisation kernels.
+#include "tau_launch.h"
+#include "tau_misc.cuh"
+
+namespace ft {
+
+constexpr int kStages = 3;
+
+void launch_refine(bool bicg, const Launch &L, cudaStream_t st)
+{
+    if (bicg)
+        sweep_kernel<OpRefine<true>, kStages>
+            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpRefine<true>, kStages>(), st>>>(L);
+    else
+        sweep_kernel<OpRefine<false>, kStages>
+            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpRefine<false>, kStages>(), st>>>(L);
+}
+
+cudaError_t configure_misc()
+{
+    cudaError_t a = cudaFuncSetAttribute(sweep_kernel<OpRefine<true>, kStages>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         sweep_dyn_smem<OpRefine<true>, kStages>());
+    cudaError_t b = cudaFuncSetAttribute(sweep_kernel<OpRefine<false>, kStages>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         sweep_dyn_smem<OpRefine<false>, kStages>());
+    return a != cudaSuccess ? a : b;
+}
+
+void launch_init64(const Launch &L, cudaStream_t st) { init64_kernel<<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L); }
+
+void launch_code(const Launch &L, cudaStream_t st) { code_kernel<<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L); }
+
+void launch_tau(int src, const Launch &L, cudaStream_t st)
+{
+    if (src == 1) tau_kernel<float><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, 0);
+    else tau_kernel<double><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, src == 2 ? 1 : 0);
+}
+
+}  // namespace ft

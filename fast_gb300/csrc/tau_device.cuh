@@ -1,0 +1,283 @@
+// Device building blocks of the matrix-free tortuosity solvers.
+//
+// The operator is the reference's 7-point finite-volume diffusion system
+// (fastlib/src/cuda/Diffusion.cuh:54-148) evaluated on the fly from a one-byte
+// stencil code per voxel instead of 7 stored coefficient arrays
+// (fastlib/src/cuda/Diffusion.cu:30-71 writes those).  All coefficients are in
+// h = 1 units: the reference's coefficients are Dface*h^2/dist = Dface*h for
+// interior faces and 2*D*h for the two Dirichlet faces; dividing A and b by h
+// leaves x, every solver scalar ratio and tau unchanged.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "tau_types.h"
+
+namespace ft {
+
+// ---------------------------------------------------------------------------
+// Coefficient tables, staged in shared memory at block start.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Coef {
+    T face[2][2];      // face coefficient by (self solid, neighbour solid)
+    T cell2[2];        // 2*D: the half-cell Dirichlet face (dist = h/2)
+    T diag_int[128];   // diagonal of an interior voxel, by code
+    T inv_int[128];    // its reciprocal
+};
+
+template <typename T>
+__device__ __forceinline__ void load_coef(Coef<T> &C, const Job &J, int tid)
+{
+    if constexpr (sizeof(T) == 8) {
+        if (tid < 128) {
+            C.diag_int[tid] = J.ddiag_int[tid];
+            C.inv_int[tid] = J.dinv_int[tid];
+        }
+        if (tid < 4) C.face[tid >> 1][tid & 1] = J.dface[tid >> 1][tid & 1];
+        if (tid < 2) C.cell2[tid] = 2.0 * J.dcell[tid];
+    } else {
+        if (tid < 128) {
+            C.diag_int[tid] = J.fdiag_int[tid];
+            C.inv_int[tid] = J.finv_int[tid];
+        }
+        if (tid < 4) C.face[tid >> 1][tid & 1] = J.fface[tid >> 1][tid & 1];
+        if (tid < 2) C.cell2[tid] = (float)(2.0 * J.dcell[tid]);
+    }
+}
+
+struct Geo {
+    int nx, ny, nz;
+    int k;     // primary axis
+    int sgn;   // +1 for *_POS, -1 for *_NEG
+    int P;     // row pitch of the state arrays, elements
+    __device__ __forceinline__ bool in(int x, int y, int z) const
+    {
+        return (unsigned)x < (unsigned)nx && (unsigned)y < (unsigned)ny && (unsigned)z < (unsigned)nz;
+    }
+    __device__ __forceinline__ bool interior(int x, int y, int z) const
+    {
+        return x > 0 && y > 0 && z > 0 && x < nx - 1 && y < ny - 1 && z < nz - 1;
+    }
+    __device__ __forceinline__ int64_t idx(int x, int y, int z) const
+    {
+        return (int64_t)x + (int64_t)P * ((int64_t)y + (int64_t)ny * (int64_t)z);
+    }
+    __device__ __forceinline__ int coord(int x, int y, int z) const { return k == 0 ? x : (k == 1 ? y : z); }
+    __device__ __forceinline__ int extent() const { return k == 0 ? nx : (k == 1 ? ny : nz); }
+};
+
+// Diagonal of voxel (x,y,z): 0 - c(X+) - c(X-) - c(Y+) - c(Y-) - c(Z+) - c(Z-),
+// the subtraction order of getSystemTopKernel (Diffusion.cuh:85-105).  A
+// face to an in-domain neighbour contributes its face coefficient; a domain
+// face on the primary axis contributes the half-cell Dirichlet term 2*D; a
+// domain face on a secondary axis is zero-flux and contributes nothing.
+template <typename T>
+__device__ __forceinline__ T diag_general(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+{
+    const int self = (code >> SELF_BIT) & 1;
+    T d = T(0);
+    if (x + 1 < g.nx) d -= C.face[self][code & 1];        else if (g.k == 0) d -= C.cell2[self];
+    if (x > 0)        d -= C.face[self][(code >> 1) & 1]; else if (g.k == 0) d -= C.cell2[self];
+    if (y + 1 < g.ny) d -= C.face[self][(code >> 2) & 1]; else if (g.k == 1) d -= C.cell2[self];
+    if (y > 0)        d -= C.face[self][(code >> 3) & 1]; else if (g.k == 1) d -= C.cell2[self];
+    if (z + 1 < g.nz) d -= C.face[self][(code >> 4) & 1]; else if (g.k == 2) d -= C.cell2[self];
+    if (z > 0)        d -= C.face[self][(code >> 5) & 1]; else if (g.k == 2) d -= C.cell2[self];
+    return d;
+}
+
+template <typename T>
+__device__ __forceinline__ T diag_at(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+{
+    if (g.interior(x, y, z)) return C.diag_int[code & 127];
+    return diag_general(C, g, code, x, y, z);
+}
+
+template <typename T>
+__device__ __forceinline__ T inv_diag_at(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+{
+    if (g.interior(x, y, z)) return C.inv_int[code & 127];
+    return T(1) / diag_general(C, g, code, x, y, z);
+}
+
+// Right-hand side b (Diffusion.cuh:108-122): on the first plane of the
+// primary axis b = -2D * cBegin, else on the last plane b = -2D * cEnd, with
+// cBegin = 1, cEnd = 0 for a positive direction and the reverse for a negative
+// one.  `else if`: a one-plane axis only gets the cBegin term.
+template <typename T>
+__device__ __forceinline__ T rhs_at(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+{
+    const int c = g.coord(x, y, z);
+    const int self = (code >> SELF_BIT) & 1;
+    if (c == 0) return (g.sgn > 0) ? -C.cell2[self] : T(0);
+    if (c == g.extent() - 1) return (g.sgn > 0) ? T(0) : -C.cell2[self];
+    return T(0);
+}
+
+// Initial guess (Diffusion.cuh:127-131): linear profile along the primary axis.
+template <typename T>
+__device__ __forceinline__ T x0_at(const Geo &g, int x, int y, int z)
+{
+    const int c = g.coord(x, y, z);
+    const T q = T(c) / T(g.extent() + 1);
+    return (g.sgn > 0) ? (T(1.0f) - q) : q;
+}
+
+// y = A f at (x,y,z) given the field at the voxel and its 6 neighbours, in
+// the reference's summation order X+,X-,Y+,Y-,Z+,Z-,diag
+// (LinearSystemDevice.cuh:67-80); faces to out-of-domain neighbours have a
+// zero (skipped) coefficient.
+template <typename T>
+__device__ __forceinline__ T apply_stencil(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z,
+                                           T fc, T fxp, T fxm, T fyp, T fym, T fzp, T fzm, T diag)
+{
+    const int self = (code >> SELF_BIT) & 1;
+    const T a = C.face[self][0], b = C.face[self][1];
+    T s = T(0);
+    if (x + 1 < g.nx) s += fxp * ((code & 1) ? b : a);
+    if (x > 0)        s += fxm * ((code & 2) ? b : a);
+    if (y + 1 < g.ny) s += fyp * ((code & 4) ? b : a);
+    if (y > 0)        s += fym * ((code & 8) ? b : a);
+    if (z + 1 < g.nz) s += fzp * ((code & 16) ? b : a);
+    if (z > 0)        s += fzm * ((code & 32) ? b : a);
+    s += fc * diag;
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Dot-product accumulation.  FP64 solves accumulate in double.  FP32 solves
+// accumulate each thread's products in FP32 (at most one slab column, a few
+// dozen terms), combine the threads of a block with compensated (two-sum)
+// FP32 arithmetic, and hand each block's (sum, error) pair to the grid level
+// as a double.  Every level has a fixed order, so reductions are
+// deterministic run to run.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Acc;
+
+template <>
+struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ double hi() const { return s; }
+    __device__ __forceinline__ double lo() const { return 0.0; }
+};
+
+template <>
+struct Acc<float> {
+    float s = 0.f;
+    __device__ __forceinline__ void add(float v) { s += v; }
+    __device__ __forceinline__ void add_prod(float a, float b) { s = fmaf(a, b, s); }
+    __device__ __forceinline__ float hi() const { return s; }
+    __device__ __forceinline__ float lo() const { return 0.f; }
+};
+
+// Error-free transformation a + b = s + e (Knuth's two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// (s, c) += (s2, c2), compensated.
+__device__ __forceinline__ void pair_add(float &s, float &c, float s2, float c2)
+{
+    float t, e;
+    two_sum(s, s2, t, e);
+    s = t;
+    c = __fadd_rn(__fadd_rn(c, c2), e);
+}
+
+// Sum NV per-thread values over the block (fixed tree) and store the block
+// totals, as doubles, to out[0..NV).  FP32 values are combined as
+// compensated (sum, error) pairs.
+template <int NV, typename V>
+__device__ __forceinline__ void block_sum_store(const V (&v)[NV], double *out, double *s_red /* [NV][2*NTHREADS/32] */)
+{
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = NTHREADS / 32;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        if constexpr (sizeof(V) == 8) {
+            double a = (double)v[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if (lane == 0) s_red[k * 2 * NW + warp] = a;
+        } else {
+            float a = (float)v[k], c = 0.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float a2 = __shfl_down_sync(0xffffffffu, a, o);
+                const float c2 = __shfl_down_sync(0xffffffffu, c, o);
+                pair_add(a, c, a2, c2);
+            }
+            if (lane == 0) {
+                s_red[k * 2 * NW + warp] = (double)a;
+                s_red[k * 2 * NW + NW + warp] = (double)c;
+            }
+        }
+    }
+    __syncthreads();
+    if (tid < NV) {
+        double a = 0.0;
+        if constexpr (sizeof(V) == 8) {
+#pragma unroll
+            for (int w = 0; w < NW; w++) a += s_red[tid * 2 * NW + w];
+        } else {
+            float s = 0.f, c = 0.f;
+#pragma unroll
+            for (int w = 0; w < NW; w++) pair_add(s, c, (float)s_red[tid * 2 * NW + w], (float)s_red[tid * 2 * NW + NW + w]);
+            a = (double)s + (double)c;
+        }
+        out[tid] = a;
+    }
+}
+
+// Arrival of a block at the end of a kernel.  Returns true (block-uniform)
+// in the last block to arrive for this job; that block then sums all
+// partials of the job, in a fixed order.
+__device__ __forceinline__ bool arrive_last(uint32_t *counter, int64_t ntiles, int *s_flag)
+{
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t prev = atomicAdd(counter, 1u);
+        *s_flag = (prev == (uint32_t)(ntiles - 1)) ? 1 : 0;
+    }
+    __syncthreads();
+    return *s_flag != 0;
+}
+
+template <int NV>
+__device__ __forceinline__ void sum_partials(const double *part, int64_t ntiles, double (&tot)[NV], double *s_red)
+{
+    const int tid = threadIdx.x;
+    __threadfence();
+    double v[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) v[k] = 0.0;
+    for (int64_t t = tid; t < ntiles; t += NTHREADS) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) v[k] += __ldcg(part + t * NPART + k);
+    }
+    __shared__ double s_tot[NV];
+    block_sum_store<NV, double>(v, s_tot, s_red);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) tot[k] = s_tot[k];
+}
+
+// Locate the job of this block (jobs are laid out back to back by tile_base).
+__device__ __forceinline__ int find_job(const Launch &L, int64_t b)
+{
+    int lo = 0, hi = L.njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (L.jobs[mid].tile_base <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+}  // namespace ft

@@ -1,0 +1,761 @@
+// Host orchestration and the C ABI of libfasttau.so.
+//
+// Replaces the reference's getTortuosity<T> driver
+// (fastlib/src/volume/VolumeMeasures.cpp:42-285): system assembly
+// (GenerateDiffusionLinearSystemDevice, fastlib/src/solver/Diffusion.cpp:
+// 177-231) becomes the one-byte stencil-code build; the solver dispatch
+// (CG.cpp:40-109, BICGSTAB.cpp:41-103) becomes fused kernels replayed from a
+// captured CUDA graph; the host tau loop (VolumeMeasures.cpp:188-275) becomes
+// a device FP64 reduction.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fasttau.h"
+#include "tau_launch.h"
+#include "tau_types.h"
+
+using namespace ft;
+
+// ---------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+static int fail(int status, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            return fail(e_ == cudaErrorMemoryAllocation ? FAST_NOMEM : FAST_CUDA_ERROR,            \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+        }                                                                                          \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Per-thread engine: one non-blocking stream per device, pinned staging.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Engine {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    Scalars *h_sc = nullptr;   // pinned, 2 * kMaxJobs (double-buffered poll)
+    Job *h_jobs = nullptr;     // pinned staging for job descriptors
+    static constexpr int kMaxJobs = 1024;
+
+    int init(int dev)
+    {
+        device = dev;
+        CU(cudaSetDevice(dev));
+        CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        CU(cudaMallocHost(&h_sc, sizeof(Scalars) * 2 * kMaxJobs));
+        CU(cudaMallocHost(&h_jobs, sizeof(Job) * kMaxJobs));
+        cudaError_t ce = configure_f64();
+        if (ce == cudaSuccess) ce = configure_f32();
+        if (ce == cudaSuccess) ce = configure_misc();
+        if (ce != cudaSuccess) return fail(FAST_CUDA_ERROR, "kernel configuration: %s", cudaGetErrorString(ce));
+        // Keep freed pool memory for reuse by the next solve.
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = std::numeric_limits<uint64_t>::max();
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        return FAST_OK;
+    }
+};
+
+thread_local Engine *t_engines[64] = {};
+
+int get_engine(Engine **out)
+{
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(FAST_CUDA_ERROR, "device ordinal %d out of range", dev);
+    if (!t_engines[dev]) {
+        Engine *e = new Engine();
+        int st = e->init(dev);
+        if (st != FAST_OK) {
+            delete e;
+            return st;
+        }
+        t_engines[dev] = e;
+    }
+    *out = t_engines[dev];
+    return FAST_OK;
+}
+
+int env_int(const char *name, int dflt)
+{
+    const char *v = getenv(name);
+    return v ? atoi(v) : dflt;
+}
+
+double env_double(const char *name, double dflt)
+{
+    const char *v = getenv(name);
+    return v ? atof(v) : dflt;
+}
+
+// Launch bookkeeping and the optional per-launch CUDA-event profile.
+struct Prof {
+    fast_tau_stats st;
+    bool on = false;
+    cudaEvent_t a = nullptr, b = nullptr;
+    void reset(bool enable)
+    {
+        memset(&st, 0, sizeof(st));
+        on = enable;
+        st.profiled = enable ? 1 : 0;
+        if (on && !a) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+        }
+    }
+};
+thread_local Prof t_prof;
+
+int kind_of(Step s)
+{
+    switch (s) {
+    case Step::INIT_CG:
+    case Step::INIT_BI: return FAST_K_INIT;
+    case Step::CG1: return FAST_K_CG1;
+    case Step::CG2: return FAST_K_CG2;
+    case Step::BI_RESTART: return FAST_K_BI_RESTART;
+    case Step::BI1: return FAST_K_BI1;
+    case Step::BI2: return FAST_K_BI2;
+    case Step::BI3: return FAST_K_BI3;
+    }
+    return FAST_K_COUNT - 1;
+}
+
+// Runs one kernel launch, counting it and, when profiling, timing it with a
+// CUDA event pair on the launching stream.
+template <class F>
+void launch_counted(int kind, cudaStream_t st, F &&f)
+{
+    Prof &P = t_prof;
+    if (!P.on) {
+        f();
+    } else {
+        cudaEventRecord(P.a, st);
+        f();
+        cudaEventRecord(P.b, st);
+        cudaEventSynchronize(P.b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, P.a, P.b);
+        P.st.kernel_ms[kind] += ms;
+    }
+    P.st.kernel_launches[kind] += 1;
+    P.st.launches += 1;
+}
+
+// Coefficient tables of one job, in h = 1 units (see tau_device.cuh).
+void fill_tables(Job &J, double d0, double d1, int face_mean)
+{
+    // Domain values as T(params.d0/d1) (LinearSystemDevice.cu:8-20).
+    const double Dd[2] = {d0, d1};
+    const float Df[2] = {(float)d0, (float)d1};
+    for (int s = 0; s < 2; s++) {
+        J.dcell[s] = Dd[s];
+        for (int n = 0; n < 2; n++) {
+            if (face_mean == FAST_FACE_HARMONIC) {
+                J.dface[s][n] = 2.0 * Dd[n] * Dd[s] / (Dd[n] + Dd[s]);
+                J.fface[s][n] = 2.0f * Df[n] * Df[s] / (Df[n] + Df[s]);
+            } else {
+                // (D(neighbour) + D(here)) * 0.5 (Diffusion.cu:47-53)
+                J.dface[s][n] = (Dd[n] + Dd[s]) * 0.5;
+                J.fface[s][n] = (Df[n] + Df[s]) * 0.5f;
+            }
+        }
+    }
+    for (int code = 0; code < 128; code++) {
+        const int self = (code >> SELF_BIT) & 1;
+        double dd = 0.0;
+        float df = 0.f;
+        for (int f = 0; f < 6; f++) {  // subtraction order of Diffusion.cuh:85-105
+            const int nb = (code >> f) & 1;
+            dd -= J.dface[self][nb];
+            df -= J.fface[self][nb];
+        }
+        J.ddiag_int[code] = dd;
+        J.dinv_int[code] = 1.0 / dd;
+        J.fdiag_int[code] = df;
+        J.finv_int[code] = 1.0f / df;
+    }
+    J.c_tau[0] = (float)d0;
+    J.c_tau[1] = (float)d1;
+}
+
+struct Geometry {
+    int64_t nx, ny, nz, N;
+    int zc, tx, ty, tz;
+    int64_t ntiles;
+};
+
+Geometry make_geometry(int64_t nx, int64_t ny, int64_t nz)
+{
+    Geometry g;
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    g.N = nx * ny * nz;
+    g.tx = (int)((nx + TX - 1) / TX);
+    g.ty = (int)((ny + TY - 1) / TY);
+    int zc = env_int("FAST_TAU_ZC", 32);
+    if (zc < 1) zc = 1;
+    if (zc > nz) zc = (int)nz;
+    g.zc = zc;
+    g.tz = (int)((nz + zc - 1) / zc);
+    g.ntiles = (int64_t)g.tx * g.ty * g.tz;
+    return g;
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Row pitch (elements) of every array of a volume: nx rounded up to 16, so a
+// row of any element size starts on a 16-byte boundary (TMA stride rule).
+int64_t row_pitch(int64_t nx) { return (nx + 15) / 16 * 16; }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::mutex g_encode_mu;
+
+int tensor_map(CUtensorMap *tm, const void *base, int es, int64_t nx, int64_t ny, int64_t nz, int64_t pitch)
+{
+    {
+        std::lock_guard<std::mutex> lk(g_encode_mu);
+        if (!g_encode) {
+            cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+            void *fn = nullptr;
+            cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+            if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+                return fail(FAST_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
+            g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+        }
+    }
+    const CUtensorMapDataType dt = es == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                 : (es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64);
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)(pitch * es), (cuuint64_t)(pitch * ny * es)};
+    // Box: the TX x TY tile plus a one-voxel halo, widened in x so that its
+    // start (x0 - 16/es) and width are multiples of 16 bytes.
+    const cuuint32_t box[3] = {(cuuint32_t)(TX + 2 * (16 / es)), (cuuint32_t)HY, 1u};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    CUresult r = g_encode(tm, dt, 3, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(FAST_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return FAST_OK;
+}
+
+// Device memory of one multi-direction solve, carved from one allocation.
+struct Arena {
+    char *base = nullptr;
+    size_t off = 0, cap = 0;
+    void *take(size_t bytes)
+    {
+        void *p = base + off;
+        off += align_up(bytes, 256);
+        return p;
+    }
+};
+
+// Replays `chunk` iterations from a captured graph until every job has left
+// RUNNING; polls the device scalars one chunk behind so the queue never
+// drains while the host waits.
+int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vector<Step> &steps,
+            void (*launch)(Step, const Launch &, cudaStream_t), uint64_t max_iter)
+{
+    cudaStream_t st = E.stream;
+    const int chunk = std::max(1, env_int("FAST_TAU_CHUNK", 16));
+    if (t_prof.on) {
+        // Profiling: direct launches, each timed; the scalars are read after
+        // every chunk.
+        const uint64_t max_chunks = max_iter / (uint64_t)chunk + 4;
+        for (uint64_t k = 0; k < max_chunks; k++) {
+            for (int c = 0; c < chunk; c++)
+                for (Step s : steps) launch_counted(kind_of(s), st, [&] { launch(s, L, st); });
+            CU(cudaMemcpyAsync(E.h_sc, d_sc, sizeof(Scalars) * njobs, cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+            bool running = false;
+            for (int j = 0; j < njobs; j++) running |= (E.h_sc[j].state == RUNNING);
+            if (!running) break;
+        }
+        return FAST_OK;
+    }
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int c = 0; c < chunk; c++)
+        for (Step s : steps) launch(s, L, st);
+    cudaError_t cerr = cudaStreamEndCapture(st, &graph);
+    if (cerr != cudaSuccess) return fail(FAST_CUDA_ERROR, "graph capture failed: %s", cudaGetErrorString(cerr));
+    cerr = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (cerr != cudaSuccess) return fail(FAST_CUDA_ERROR, "graph instantiate failed: %s", cudaGetErrorString(cerr));
+
+    cudaEvent_t ev[2];
+    cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+    const uint64_t max_chunks = max_iter / (uint64_t)chunk + 4;
+    int status = FAST_OK;
+    uint64_t k = 0;
+    for (; k < max_chunks; k++) {
+        cerr = cudaGraphLaunch(exec, st);
+        if (cerr != cudaSuccess) { status = fail(FAST_CUDA_ERROR, "graph launch: %s", cudaGetErrorString(cerr)); break; }
+        t_prof.st.graph_replays += 1;
+        t_prof.st.launches += (uint64_t)chunk * steps.size();
+        for (Step s : steps) t_prof.st.kernel_launches[kind_of(s)] += (uint64_t)chunk;
+        Scalars *hb = E.h_sc + (k & 1) * Engine::kMaxJobs;
+        cudaMemcpyAsync(hb, d_sc, sizeof(Scalars) * njobs, cudaMemcpyDeviceToHost, st);
+        cudaEventRecord(ev[k & 1], st);
+        if (k == 0) continue;
+        cerr = cudaEventSynchronize(ev[(k - 1) & 1]);
+        if (cerr != cudaSuccess) { status = fail(FAST_CUDA_ERROR, "solver step: %s", cudaGetErrorString(cerr)); break; }
+        const Scalars *prev = E.h_sc + ((k - 1) & 1) * Engine::kMaxJobs;
+        bool running = false;
+        for (int j = 0; j < njobs; j++) running |= (prev[j].state == RUNNING);
+        if (!running) break;
+    }
+    cerr = cudaStreamSynchronize(st);
+    if (cerr != cudaSuccess && status == FAST_OK) status = fail(FAST_CUDA_ERROR, "solver: %s", cudaGetErrorString(cerr));
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    cudaGraphExecDestroy(exec);
+    return status;
+}
+
+void dispatch_f64(Step s, const Launch &L, cudaStream_t st) { launch_pure_f64(s, L, st); }
+void dispatch_f32(Step s, const Launch &L, cudaStream_t st) { launch_pure_f32(s, L, st); }
+void dispatch_mixed(Step s, const Launch &L, cudaStream_t st) { launch_mixed_inner(s, L, st); }
+
+int status_of(int state)
+{
+    switch (state) {
+    case CONVERGED: return FAST_OK;
+    case DIVERGED: return FAST_DIVERGED;
+    case STALLED: return FAST_NO_CONVERGENCE;
+    case FAULT: return FAST_TIMEOUT;
+    case RUNNING: return FAST_TIMEOUT;
+    default: return FAST_NO_CONVERGENCE;  // MAXITER, ZERO_RHS (CG.cu:41-44 returns false)
+    }
+}
+
+// The whole multi-direction solve on a device-resident mask.
+int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, const fast_tau_params &P,
+                 int ndirs, const int32_t *dirs, fast_tau_result *res, void *conc_out)
+{
+    cudaStream_t st = E.stream;
+    t_prof.reset((P.flags & FAST_FLAG_PROFILE) != 0);
+    const int prec = P.precision, solver = P.solver;
+    const Geometry G = make_geometry(nx, ny, nz);
+    const int64_t N = G.N;
+    const bool mixed = prec == FAST_PREC_MIXED;
+
+    // --- memory plan (the reference's fit check, VolumeMeasures.cpp:104-125)
+    const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
+    const int64_t pitch = row_pitch(nx);
+    const int64_t NP = pitch * ny * nz;  // padded element count of every array
+    const size_t vbytes = align_up((size_t)NP * vec_t, 256);
+    const size_t v64 = align_up((size_t)NP * 8, 256);
+    const size_t nvec = (solver == FAST_SOLVER_CG) ? 4 : 8;
+    const size_t part_bytes = align_up((size_t)G.ntiles * NPART * sizeof(double), 256);
+    size_t need = align_up((size_t)NP, 256)                                 // stencil codes
+                  + (size_t)ndirs * (nvec * vbytes + (mixed ? 2 * v64 : 0) + part_bytes)
+                  + align_up(sizeof(Scalars) * ndirs, 256) + align_up(sizeof(uint32_t) * ndirs, 256)
+                  + align_up(sizeof(Job) * ndirs, 256) + 4096;
+    size_t free_b = 0, total_b = 0;
+    CU(cudaMemGetInfo(&free_b, &total_b));
+    if (need > free_b) {
+        // Memory already cached by the stream-ordered pool counts as available.
+        size_t reserved = 0;
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, E.device) == cudaSuccess) {
+            uint64_t r = 0, u = 0;
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r);
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u);
+            reserved = (size_t)(r - u);
+        }
+        if (need > free_b + reserved)
+            return fail(FAST_NOMEM, "Solver will not fit in GPU memory: needs %.3f GB, %.3f GB free", need / 1e9,
+                        (free_b + reserved) / 1e9);
+    }
+    (void)total_b;
+
+    Arena A;
+    CU(cudaMallocAsync((void **)&A.base, need, st));
+    A.cap = need;
+    uint8_t *d_code = (uint8_t *)A.take((size_t)NP);
+    Scalars *d_sc = (Scalars *)A.take(sizeof(Scalars) * ndirs);
+    uint32_t *d_cnt = (uint32_t *)A.take(sizeof(uint32_t) * ndirs);
+    Job *d_jobs = (Job *)A.take(sizeof(Job) * ndirs);
+
+    // --- job descriptors
+    int64_t maxdim = std::max(nx, std::max(ny, nz));
+    const float h = 1.0f / (float)maxdim;  // cellDim = vec3(1.0f / maxDim) (VolumeMeasures.cpp:68)
+    const double h2 = (double)h * (double)h;
+    Job *hj = E.h_jobs;
+    Scalars *hs = E.h_sc;  // staging (the poll buffers are not in use yet)
+    memset(hj, 0, sizeof(Job) * ndirs);
+    memset(hs, 0, sizeof(Scalars) * ndirs);
+    for (int j = 0; j < ndirs; j++) {
+        Job &J = hj[j];
+        J.nx = (int32_t)nx; J.ny = (int32_t)ny; J.nz = (int32_t)nz;
+        J.pitch = (int32_t)pitch;
+        J.dir = dirs[j];
+        J.tiles_x = G.tx; J.tiles_y = G.ty; J.tiles_z = G.tz;
+        J.zc = G.zc;
+        J.tile_base = (int64_t)j * G.ntiles;
+        J.ntiles = G.ntiles;
+        J.code = d_code;
+        J.mask = d_mask;
+        J.x = A.take(vbytes);
+        J.r[0] = A.take(vbytes);
+        J.p[0] = A.take(vbytes);
+        J.p[1] = A.take(vbytes);
+        if (solver == FAST_SOLVER_BICGSTAB) {
+            J.r[1] = A.take(vbytes);
+            J.r0 = A.take(vbytes);
+            J.v[0] = A.take(vbytes);
+            J.v[1] = A.take(vbytes);
+        }
+        if (mixed) {
+            J.x64[0] = (double *)A.take(v64);
+            J.x64[1] = (double *)A.take(v64);
+        }
+        J.part = (double *)A.take(part_bytes);
+        {
+            const int es = (int)vec_t;
+            int ts = tensor_map(&J.tm[TM_CODE], d_code, 1, nx, ny, nz, pitch);
+            if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_X], J.x, es, nx, ny, nz, pitch);
+            if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R], J.r[0], es, nx, ny, nz, pitch);
+            if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P], J.p[0], es, nx, ny, nz, pitch);
+            if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P + 1], J.p[1], es, nx, ny, nz, pitch);
+            if (ts == FAST_OK && solver == FAST_SOLVER_BICGSTAB) {
+                ts = tensor_map(&J.tm[TM_R + 1], J.r[1], es, nx, ny, nz, pitch);
+                if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R0], J.r0, es, nx, ny, nz, pitch);
+                if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_V], J.v[0], es, nx, ny, nz, pitch);
+                if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_V + 1], J.v[1], es, nx, ny, nz, pitch);
+            }
+            if (ts == FAST_OK && mixed) {
+                ts = tensor_map(&J.tm[TM_X64], J.x64[0], 8, nx, ny, nz, pitch);
+                if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_X64 + 1], J.x64[1], 8, nx, ny, nz, pitch);
+            }
+            if (ts != FAST_OK) {
+                cudaFreeAsync(A.base, st);
+                cudaStreamSynchronize(st);
+                return ts;
+            }
+        }
+        J.sc = d_sc + j;
+        J.counter = d_cnt + j;
+        fill_tables(J, P.d0, P.d1, P.face_mean);
+
+        Scalars &S = hs[j];
+        // Solver tolerance is T-typed (Solver.h:155-158).
+        S.tol = (prec == FAST_PREC_F32) ? (double)(float)P.tolerance : P.tolerance;
+        S.max_iter = P.max_iter;
+        S.div_thresh = 10e+10 / h2;  // |r|^2 > 1e11 in the reference's h-scaled units
+        S.eps2 = (prec == FAST_PREC_F64) ? (double)DBL_EPSILON * DBL_EPSILON
+                                         : (double)FLT_EPSILON * (double)FLT_EPSILON;
+        S.state = mixed ? CONVERGED : RUNNING;
+        S.tol_outer = P.tolerance;
+        S.inner_floor = env_double("FAST_TAU_INNER_TOL", 1e-4);
+        S.max_total = P.max_iter;
+        S.outer_state = RUNNING;
+        S.inner_mode = mixed ? 1 : 0;
+    }
+    CU(cudaMemcpyAsync(d_jobs, hj, sizeof(Job) * ndirs, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_sc, hs, sizeof(Scalars) * ndirs, cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t) * ndirs, st));
+    // The staging buffers are reused below: wait for the copies to land.
+    CU(cudaStreamSynchronize(st));
+
+    Launch L{d_jobs, ndirs, 0, (int64_t)ndirs * G.ntiles};
+    Launch L1{d_jobs, 1, 0, G.ntiles};  // the volume itself (codes + porosity)
+
+    int status = FAST_OK;
+    launch_counted(FAST_K_CODE, st, [&] { launch_code(L1, st); });
+    if (!mixed) {
+        void (*fn)(Step, const Launch &, cudaStream_t) = (prec == FAST_PREC_F64) ? dispatch_f64 : dispatch_f32;
+        launch_counted(FAST_K_INIT, st, [&] { fn(solver == FAST_SOLVER_CG ? Step::INIT_CG : Step::INIT_BI, L, st); });
+        std::vector<Step> steps;
+        if (solver == FAST_SOLVER_CG) steps = {Step::CG1, Step::CG2};
+        else steps = {Step::BI_RESTART, Step::BI1, Step::BI2, Step::BI3};
+        status = iterate(E, L, ndirs, d_sc, steps, fn, P.max_iter);
+    } else {
+        launch_counted(FAST_K_INIT64, st, [&] { launch_init64(L, st); });
+        std::vector<Step> steps;
+        if (solver == FAST_SOLVER_CG) steps = {Step::CG1, Step::CG2};
+        else steps = {Step::BI_RESTART, Step::BI1, Step::BI2, Step::BI3};
+        const int max_outer = env_int("FAST_TAU_MAX_OUTER", 60);
+        for (int o = 0; o < max_outer && status == FAST_OK; o++) {
+            launch_counted(FAST_K_REFINE, st, [&] { launch_refine(solver == FAST_SOLVER_BICGSTAB, L, st); });
+            CU(cudaMemcpyAsync(hs, d_sc, sizeof(Scalars) * ndirs, cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+            bool running = false, inner = false;
+            for (int j = 0; j < ndirs; j++) {
+                running |= hs[j].outer_state == RUNNING;
+                inner |= hs[j].state == RUNNING;
+            }
+            if (!running) break;
+            // e = 0 for the next inner solve, and for a rejected correction.
+            for (int j = 0; j < ndirs; j++)
+                if (hs[j].outer_state == RUNNING)
+                    CU(cudaMemsetAsync(hj[j].x, 0, (size_t)NP * sizeof(float), st));
+            if (inner) status = iterate(E, L, ndirs, d_sc, steps, dispatch_mixed, P.max_iter);
+        }
+    }
+    if (status == FAST_OK)
+        launch_counted(FAST_K_TAU, st, [&] { launch_tau(mixed ? 2 : (prec == FAST_PREC_F32 ? 1 : 0), L, st); });
+    CU(cudaMemcpyAsync(hs, d_sc, sizeof(Scalars) * ndirs, cudaMemcpyDeviceToHost, st));
+    if (conc_out && ndirs == 1) {
+        const void *src = hj[0].x;
+        size_t es = vec_t;
+        CU(cudaStreamSynchronize(st));
+        if (mixed) {
+            src = hj[0].x64[hs[0].x64_cur];
+            es = 8;
+        }
+        // de-pad the rows: host layout is x-fastest with pitch nx
+        CU(cudaMemcpy2DAsync(conc_out, (size_t)nx * es, src, (size_t)pitch * es, (size_t)nx * es, (size_t)(ny * nz),
+                             cudaMemcpyDeviceToHost, st));
+    }
+    cudaError_t ferr = cudaFreeAsync(A.base, st);
+    CU(cudaStreamSynchronize(st));
+    if (ferr != cudaSuccess) return fail(FAST_CUDA_ERROR, "cudaFreeAsync: %s", cudaGetErrorString(ferr));
+    if (status != FAST_OK) return status;
+
+    // --- results (the stencil-code pass counted the pores into job 0)
+    const uint64_t pores = hs[0].pores;
+    int first_bad = FAST_OK;
+    for (int j = 0; j < ndirs; j++) {
+        Scalars &S = hs[j];
+        S.pores = pores;
+        fast_tau_result &R = res[j];
+        memset(&R, 0, sizeof(R));
+        const int state = mixed ? S.outer_state : S.state;
+        R.status = status_of(state);
+        R.iterations = mixed ? S.total_iter : S.iter;
+        R.outer_steps = mixed ? (uint32_t)S.outer_steps : 0;
+        if (mixed) R.rel_residual = S.b64_sq > 0 ? std::sqrt(S.r64_sq / S.b64_sq) : 0.0;
+        else R.rel_residual = S.rhs_sq > 0 ? std::sqrt(S.rsq / S.rhs_sq) : 0.0;
+        // Porosity: precomputed by the caller, or getPorosity<T> (VolumeMeasures.cpp:179-181).
+        const int k = dirs[j] >> 1;
+        const int64_t dimk = k == 0 ? nx : (k == 1 ? ny : nz);
+        const int64_t nplane = N / dimk;
+        if (prec == FAST_PREC_F32) {
+            const float phi = P.porosity >= 0 ? (float)P.porosity : (float)S.pores / (float)N;
+            R.porosity = phi;
+            // tau = porosity / (dc * n_k), dc = sum over planes of (plane sum / n) / n_k
+            const float S32 = (float)S.flux_sum;
+            const float dc = (S32 / (float)nplane) / (float)dimk;
+            R.tau = (R.status == FAST_OK) ? (double)(phi / (dc * (float)dimk)) : 0.0;
+        } else {
+            const double phi = P.porosity >= 0 ? P.porosity : (double)S.pores / (double)N;
+            R.porosity = phi;
+            const double dc = (S.flux_sum / (double)nplane) / (double)dimk;
+            R.tau = (R.status == FAST_OK) ? phi / (dc * (double)dimk) : 0.0;
+        }
+        if (R.status != FAST_OK && first_bad == FAST_OK) {
+            first_bad = R.status;
+            fail(R.status, "direction %d: solver %s after %llu iterations (|r|/|b| = %.3e)", dirs[j],
+                 R.status == FAST_DIVERGED ? "diverged" : "did not converge",
+                 (unsigned long long)R.iterations, R.rel_residual);
+        }
+        if (P.verbose)
+            fprintf(stderr, "fasttau: dir %d tau %.10g iters %llu outer %u relres %.3e status %d\n", dirs[j], R.tau,
+                    (unsigned long long)R.iterations, R.outer_steps, R.rel_residual, R.status);
+    }
+    return first_bad;
+}
+
+int check_args(const void *mask, int64_t nx, int64_t ny, int64_t nz, const fast_tau_params *p, int ndirs,
+               const int32_t *dirs)
+{
+    if (!mask) return fail(FAST_NO_HOST_DATA, "mask must be allocated (VolumeMeasures.cpp:55)");
+    if (!p) return fail(FAST_BAD_ARG, "params is NULL");
+    if (nx <= 0 || ny <= 0 || nz <= 0) return fail(FAST_BAD_ARG, "dimensions must be positive");
+    if (nx > INT32_MAX / 2 || ny > INT32_MAX / 2 || nz > INT32_MAX / 2)
+        return fail(FAST_BAD_ARG, "dimension too large");
+    const Geometry G = make_geometry(nx, ny, nz);
+    if (G.ntiles * (int64_t)std::max(ndirs, 1) > (int64_t)INT32_MAX) return fail(FAST_BAD_ARG, "volume too large");
+    if (p->solver != FAST_SOLVER_BICGSTAB && p->solver != FAST_SOLVER_CG)
+        return fail(FAST_BAD_ARG, "Unknown solver %d", p->solver);
+    if (p->precision < FAST_PREC_F64 || p->precision > FAST_PREC_MIXED)
+        return fail(FAST_BAD_ARG, "unknown precision %d", p->precision);
+    if (p->face_mean != FAST_FACE_ARITHMETIC && p->face_mean != FAST_FACE_HARMONIC)
+        return fail(FAST_BAD_ARG, "unknown face mean %d", p->face_mean);
+    if (!(p->tolerance >= 0.0)) return fail(FAST_BAD_ARG, "tolerance must be >= 0");
+    if (!(p->d0 > 0.0) || !(p->d1 > 0.0)) return fail(FAST_BAD_ARG, "diffusivities must be positive");
+    if (ndirs < 1 || ndirs > 6 || !dirs) return fail(FAST_BAD_ARG, "need 1..6 directions");
+    for (int j = 0; j < ndirs; j++)
+        if (dirs[j] < 0 || dirs[j] > 5) return fail(FAST_BAD_ARG, "bad direction %d", dirs[j]);
+    return FAST_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+FAST_API const char *fast_last_error(void) { return g_last_error.c_str(); }
+
+FAST_API const char *fast_version(void) { return "fasttau 0.1 (sm_103a)"; }
+
+FAST_API int fast_tau_last_stats(fast_tau_stats *out)
+{
+    if (!out) return fail(FAST_BAD_ARG, "stats is NULL");
+    *out = t_prof.st;
+    return FAST_OK;
+}
+
+FAST_API void fast_tau_params_init(fast_tau_params *p)
+{
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->dir = FAST_X_NEG;
+    p->solver = FAST_SOLVER_BICGSTAB;
+    p->precision = FAST_PREC_F64;
+    p->face_mean = FAST_FACE_ARITHMETIC;
+    p->tolerance = 1e-6;
+    p->max_iter = 10000;
+    p->d0 = (double)1.0f;
+    p->d1 = (double)0.001f;
+    p->porosity = -1.0;
+}
+
+FAST_API int fast_tau_solve_dirs_device(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz,
+                                        const fast_tau_params *p, int32_t ndirs, const int32_t *dirs,
+                                        fast_tau_result *results, void *stream)
+{
+    g_last_error.clear();
+    int st = check_args(d_mask, nx, ny, nz, p, ndirs, dirs);
+    if (st != FAST_OK) return st;
+    if (!results) return fail(FAST_BAD_ARG, "results is NULL");
+    Engine *E = nullptr;
+    st = get_engine(&E);
+    if (st != FAST_OK) return st;
+    cudaStream_t saved = E->stream;
+    if (stream) E->stream = (cudaStream_t)stream;
+    st = solve_device(*E, d_mask, nx, ny, nz, *p, ndirs, dirs, results, nullptr);
+    E->stream = saved;
+    return st;
+}
+
+static int solve_host(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, const fast_tau_params *p,
+                      int32_t ndirs, const int32_t *dirs, fast_tau_result *results, void *conc_out)
+{
+    g_last_error.clear();
+    int st = check_args(mask, nx, ny, nz, p, ndirs, dirs);
+    if (st != FAST_OK) return st;
+    Engine *E = nullptr;
+    st = get_engine(&E);
+    if (st != FAST_OK) return st;
+    const size_t N = (size_t)(nx * ny * nz);
+    uint8_t *d_mask = nullptr;
+    CU(cudaMallocAsync((void **)&d_mask, N, E->stream));
+    cudaError_t e = cudaMemcpyAsync(d_mask, mask, N, cudaMemcpyHostToDevice, E->stream);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(d_mask, E->stream);
+        return fail(FAST_CUDA_ERROR, "mask upload: %s", cudaGetErrorString(e));
+    }
+    st = solve_device(*E, d_mask, nx, ny, nz, *p, ndirs, dirs, results, conc_out);
+    cudaFreeAsync(d_mask, E->stream);
+    cudaStreamSynchronize(E->stream);
+    return st;
+}
+
+FAST_API int fast_tau_solve_dirs(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz,
+                                 const fast_tau_params *p, int32_t ndirs, const int32_t *dirs,
+                                 fast_tau_result *results)
+{
+    if (!results) return fail(FAST_BAD_ARG, "results is NULL");
+    return solve_host(mask, nx, ny, nz, p, ndirs, dirs, results, nullptr);
+}
+
+FAST_API int fast_tau_solve(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, const fast_tau_params *p,
+                            double *tau, uint64_t *iters, double *rel_err, void *conc_out)
+{
+    if (tau) *tau = 0.0;
+    if (!p) return fail(FAST_BAD_ARG, "params is NULL");
+    fast_tau_result r;
+    memset(&r, 0, sizeof(r));
+    const int32_t dir = p->dir;
+    int st = solve_host(mask, nx, ny, nz, p, 1, &dir, &r, conc_out);
+    if (tau) *tau = r.tau;
+    if (iters) *iters = r.iterations;
+    if (rel_err) *rel_err = r.rel_residual;
+    return st;
+}
+
+FAST_API int fast_porosity(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, double *porosity,
+                           uint64_t *pore_count)
+{
+    g_last_error.clear();
+    if (!mask) return fail(FAST_NO_HOST_DATA, "mask must be allocated");
+    if (nx <= 0 || ny <= 0 || nz <= 0) return fail(FAST_BAD_ARG, "dimensions must be positive");
+    Engine *E = nullptr;
+    int st = get_engine(&E);
+    if (st != FAST_OK) return st;
+    const Geometry G = make_geometry(nx, ny, nz);
+    const size_t N = (size_t)G.N;
+    const int64_t P = row_pitch(nx);
+    const size_t NP = (size_t)(P * ny * nz);
+    cudaStream_t s = E->stream;
+    Arena A;
+    const size_t need = align_up(N, 256) + align_up(NP, 256) + align_up((size_t)G.ntiles * NPART * 8, 256) + 4 * 4096;
+    CU(cudaMallocAsync((void **)&A.base, need, s));
+    uint8_t *d_mask = (uint8_t *)A.take(N);
+    uint8_t *d_code = (uint8_t *)A.take(NP);
+    double *d_part = (double *)A.take((size_t)G.ntiles * NPART * 8);
+    Scalars *d_sc = (Scalars *)A.take(sizeof(Scalars));
+    uint32_t *d_cnt = (uint32_t *)A.take(sizeof(uint32_t));
+    Job *d_job = (Job *)A.take(sizeof(Job));
+    Job &J = E->h_jobs[0];
+    memset(&J, 0, sizeof(Job));
+    J.nx = (int32_t)nx; J.ny = (int32_t)ny; J.nz = (int32_t)nz;
+    J.pitch = (int32_t)P;
+    J.tiles_x = G.tx; J.tiles_y = G.ty; J.tiles_z = G.tz; J.zc = G.zc;
+    J.ntiles = G.ntiles;
+    J.code = d_code; J.mask = d_mask; J.part = d_part; J.sc = d_sc; J.counter = d_cnt;
+    CU(cudaMemcpyAsync(d_mask, mask, N, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(d_job, &J, sizeof(Job), cudaMemcpyHostToDevice, s));
+    CU(cudaMemsetAsync(d_sc, 0, sizeof(Scalars), s));
+    CU(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t), s));
+    Launch L{d_job, 1, 0, G.ntiles};
+    launch_code(L, s);
+    CU(cudaMemcpyAsync(E->h_sc, d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    cudaFreeAsync(A.base, s);
+    CU(cudaStreamSynchronize(s));
+    const uint64_t pores = E->h_sc[0].pores;
+    if (pore_count) *pore_count = pores;
+    if (porosity) *porosity = (double)pores / (double)N;
+    return FAST_OK;
+}
+
+}  // extern "C"

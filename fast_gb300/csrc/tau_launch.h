@@ -1,0 +1,28 @@
+// Host-side launchers of the device kernels (one translation unit per
+// precision family so the build compiles them in parallel).
+#pragma once
+#include <cuda_runtime.h>
+#include "tau_types.h"
+
+namespace ft {
+
+enum class Step { INIT_CG, INIT_BI, CG1, CG2, BI_RESTART, BI1, BI2, BI3 };
+
+// Pure-precision solves: `f64` selects double, otherwise float (scalars in
+// the solve precision, as the reference's T).
+void launch_pure_f64(Step s, const Launch &L, cudaStream_t st);
+void launch_pure_f32(Step s, const Launch &L, cudaStream_t st);
+// FP32 inner iterations of a MIXED solve (scalars in double).
+void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st);
+// FP64 refinement step of a MIXED solve.
+void launch_refine(bool bicg, const Launch &L, cudaStream_t st);
+void launch_init64(const Launch &L, cudaStream_t st);
+void launch_code(const Launch &L, cudaStream_t st);
+// tau flux sum: src 0 = double x, 1 = float x, 2 = the current FP64 iterate.
+void launch_tau(int src, const Launch &L, cudaStream_t st);
+// Raise the dynamic shared-memory limit of every sweep kernel (once per device).
+cudaError_t configure_f64();
+cudaError_t configure_f32();
+cudaError_t configure_misc();
+
+}  // namespace ft

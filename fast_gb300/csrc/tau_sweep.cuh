@@ -1,0 +1,891 @@
+// The z-marching stencil sweep shared by every solver kernel, and the
+// operations (Op) that plug into it.
+//
+// One thread block owns a TX x TY column tile of one right-hand side and
+// marches the planes z0..z1-1 of its slab.  The state vectors an operation
+// reads arrive through TMA: for every plane, thread 0 issues one
+// cp.async.bulk.tensor tile load per vector (the TX x TY tile plus a
+// one-voxel x/y halo, widened in x to the 16-byte TMA alignment) into a ring
+// of NSTAGE shared-memory stages, each completed on its own mbarrier, so
+// NSTAGE-1 planes of every vector are in flight while the block computes.
+// From a stage the block forms the operand field of the plane (p = z + beta
+// p, y = p/diag, ...) for its tile and halo into a shared plane buffer; the z
+// neighbours of a thread's own column stay in registers.  The operator is
+// applied one plane behind the loads.  Dot products accumulate per thread,
+// reduce per block into a partial slot, and the last block of each
+// right-hand side to arrive sums the partials in a fixed order and advances
+// that right-hand side's scalars.
+//
+// Every mbarrier wait is bounded (%globaltimer, 2 s).  A block whose tile
+// loads do not arrive drains its own copies in flight (again bounded), marks
+// its job FAULT and returns; the host reports FAST_TIMEOUT.
+#pragma once
+#include "tau_device.cuh"
+
+namespace ft {
+
+// ---------------------------------------------------------------------------
+// TMA / mbarrier primitives (inline PTX).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_timer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
+
+// Waits for phase `parity` of the mbarrier, giving up after kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_timer_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (global_timer_ns() - t0 > kWaitLimitNs) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *tm, int x, int y, int z, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(dst), "l"(tm), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tmap(const CUtensorMap *tm)
+{
+    asm volatile("prefetch.tensormap [%0];" ::"l"(tm) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory stage layout.  A stream of element size ES is loaded as a box
+// of box_w(ES) x HY elements starting at (x0 - 16/ES, y0 - 1): the box start
+// and width in x are multiples of 16 bytes.
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int box_off(int es) { return 16 / es; }
+__host__ __device__ constexpr int box_w(int es) { return TX + 2 * box_off(es); }
+__host__ __device__ constexpr int box_bytes(int es) { return box_w(es) * HY * es; }
+__host__ __device__ constexpr int box_alloc(int es) { return (box_bytes(es) + 127) / 128 * 128; }
+
+template <int... ES>
+struct Streams {
+    static constexpr int N = sizeof...(ES);
+    __host__ __device__ static constexpr int esz(int s)
+    {
+        constexpr int a[N] = {ES...};
+        return a[s];
+    }
+    __host__ __device__ static constexpr int off(int s)
+    {
+        int o = 0;
+        for (int t = 0; t < s; ++t) o += box_alloc(esz(t));
+        return o;
+    }
+    __host__ __device__ static constexpr int stage_bytes() { return off(N); }
+    __host__ __device__ static constexpr int tx_bytes()
+    {
+        int b = 0;
+        for (int t = 0; t < N; ++t) b += box_bytes(esz(t));
+        return b;
+    }
+};
+
+// A point of the stage tile: its element offset within a box of each
+// element size, for tile row `row` (0..HY-1) and x offset xr = x - x0 (-1..TX).
+struct Pt {
+    int o1, o4, o8;
+};
+__device__ __forceinline__ Pt make_pt(int row, int xr)
+{
+    return Pt{row * box_w(1) + xr + box_off(1), row * box_w(4) + xr + box_off(4), row * box_w(8) + xr + box_off(8)};
+}
+
+// Element of stream S at point p of a stage.
+template <typename E, class SL, int S>
+__device__ __forceinline__ E sv(const unsigned char *stage, const Pt &p)
+{
+    constexpr int es = (int)sizeof(E);
+    const int o = es == 1 ? p.o1 : (es == 4 ? p.o4 : p.o8);
+    return reinterpret_cast<const E *>(stage + SL::off(S))[o];
+}
+
+// Diagonal, its inverse and the operator on the interior fast path (all six
+// neighbours inside the domain: table lookups, no boundary tests) or the
+// general path.
+template <typename T, bool INT>
+__device__ __forceinline__ T diag_x(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+{
+    if constexpr (INT) return C.diag_int[code & 127];
+    else return diag_at<T>(C, g, code, x, y, z);
+}
+template <typename T, bool INT>
+__device__ __forceinline__ T inv_x(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+{
+    if constexpr (INT) return C.inv_int[code & 127];
+    else return inv_x<T, INT>(C, g, code, x, y, z);
+}
+template <typename T, bool INT>
+__device__ __forceinline__ T stencil_x(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z, T fc,
+                                       T fxp, T fxm, T fyp, T fym, T fzp, T fzm, T diag)
+{
+    if constexpr (INT) {
+        const int self = (code >> SELF_BIT) & 1;
+        const T a = C.face[self][0], b = C.face[self][1];
+        T s = fxp * ((code & 1) ? b : a);
+        s += fxm * ((code & 2) ? b : a);
+        s += fyp * ((code & 4) ? b : a);
+        s += fym * ((code & 8) ? b : a);
+        s += fzp * ((code & 16) ? b : a);
+        s += fzm * ((code & 32) ? b : a);
+        s += fc * diag;
+        return s;
+    } else {
+        return apply_stencil<T>(C, g, code, x, y, z, fc, fxp, fxm, fyp, fym, fzp, fzm, diag);
+    }
+}
+
+// Halo slot h (0..NHALO-1) of the shared plane -> (hx, hy) in the buffer.
+__device__ __forceinline__ void halo_slot(int h, int &hx, int &hy)
+{
+    if (h < HX) { hx = h; hy = 0; }
+    else if (h < 2 * HX) { hx = h - HX; hy = HY - 1; }
+    else if (h < 2 * HX + TY) { hx = 0; hy = 1 + (h - 2 * HX); }
+    else { hx = HX - 1; hy = 1 + (h - 2 * HX - TY); }
+}
+constexpr int NHALO = 2 * HX + 2 * TY;
+
+// Dynamic shared memory of a sweep: the stage ring plus 128 bytes to align
+// its base to 128 bytes.
+template <class Op, int NSTAGE>
+__host__ __device__ constexpr int sweep_dyn_smem()
+{
+    return NSTAGE * Op::SL::stage_bytes() + 128;
+}
+
+template <class Op, int NSTAGE>
+__global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
+{
+    using T = typename Op::T;
+    using SL = typename Op::SL;
+    constexpr int NV = Op::NV;
+    constexpr int SB = SL::stage_bytes();
+    extern __shared__ __align__(128) unsigned char dsm[];
+    __shared__ __align__(8) uint64_t bars[NSTAGE];
+    __shared__ int s_job, s_go, s_flag, s_err;
+    __shared__ Coef<T> C;
+    __shared__ T fb[3][HY][HX];
+    __shared__ double s_red[2 * NV * (NTHREADS / 32)];
+    __shared__ typename Op::Shared S;
+
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        s_job = find_job(L, (int64_t)blockIdx.x);
+        s_go = Op::active(*L.jobs[s_job].sc) ? 1 : 0;
+        s_err = 0;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const Job &J = L.jobs[s_job];
+    load_coef<T>(C, J, tid);
+    Op::load_shared(S, J, tid);
+
+    const Geo g{J.nx, J.ny, J.nz, J.dir >> 1, (J.dir & 1) ? -1 : 1, J.pitch};
+    const int64_t local = (int64_t)blockIdx.x - J.tile_base;
+    const int tx_t = (int)(local % J.tiles_x);
+    const int ty_t = (int)((local / J.tiles_x) % J.tiles_y);
+    const int tz_t = (int)(local / ((int64_t)J.tiles_x * J.tiles_y));
+    const int x0 = tx_t * TX, y0 = ty_t * TY;
+    const int z0 = tz_t * J.zc;
+    const int z1 = min(z0 + J.zc, g.nz);
+    const int pa = max(z0 - 1, 0), pb = min(z1, g.nz - 1);
+    const int NP = pb - pa + 1;
+    const int lx = tid % TX, ly = tid / TX;
+    const int gx = x0 + lx, gy = y0 + ly;
+    const bool vxy = gx < g.nx && gy < g.ny;
+    // The tile and its halo ring lie strictly inside the domain in x and y:
+    // planes away from the z faces then take the interior fast path.
+    const bool blk_int = x0 >= 2 && x0 + TX <= g.nx - 2 && y0 >= 2 && y0 + TY <= g.ny - 2;
+    const int64_t plane = (int64_t)g.P * g.ny;
+    const int64_t i_col = (int64_t)gx + (int64_t)g.P * gy;
+
+    Op op;
+    op.init(J, S);
+
+    const uint32_t raw0 = smem_u32(dsm);
+    const uint32_t stage0 = (raw0 + 127u) & ~127u;
+    unsigned char *const sbase = dsm + (stage0 - raw0);
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+#pragma unroll
+        for (int s = 0; s < SL::N; ++s) prefetch_tmap(op.tmap[s]);
+    }
+    __syncthreads();
+    // Tile loads of plane pa+q into stage q % NSTAGE (thread 0 only).
+    auto issue = [&](int q) {
+        const int st = q % NSTAGE;
+        const uint32_t bar = smem_u32(&bars[st]);
+        mbar_arrive_expect_tx(bar, (uint32_t)SL::tx_bytes());
+#pragma unroll
+        for (int s = 0; s < SL::N; ++s)
+            tma_load_3d(stage0 + st * SB + SL::off(s), op.tmap[s], x0 - box_off(SL::esz(s)), y0 - 1, pa + q, bar);
+    };
+    if (tid == 0) {
+        const int n0 = min(NSTAGE, NP);
+        for (int q = 0; q < n0; ++q) issue(q);
+    }
+
+    int hx = 0, hy = 0, hgx = 0, hgy = 0;
+    const bool has_halo = tid < NHALO;
+    if (has_halo) {
+        halo_slot(tid, hx, hy);
+        hgx = x0 - 1 + hx;
+        hgy = y0 - 1 + hy;
+    }
+    const Pt p_own = make_pt(ly + 1, lx);
+    const Pt p_halo = make_pt(hy, hx - 1);
+    const bool halo_in = has_halo && (unsigned)hgx < (unsigned)g.nx && (unsigned)hgy < (unsigned)g.ny;
+
+    T f_m = T(0), f_c = T(0), f_p = T(0);
+    typename Op::Own o_c{}, o_p{};
+    int q = 0;
+    for (; q < NP; ++q) {
+        const int zq = pa + q;
+        const int st = q % NSTAGE;
+        if (!mbar_wait_bounded(smem_u32(&bars[st]), (uint32_t)((q / NSTAGE) & 1))) s_err = 1;
+        const unsigned char *stage = sbase + st * SB;
+        const bool out_plane = zq >= z0 && zq < z1;
+        const bool fint = blk_int && zq >= 1 && zq <= g.nz - 2;
+        if (fint) {
+            if (out_plane) o_p = op.template own<true>(g, C, S, stage, p_own, gx, gy, zq, f_p);
+            else f_p = op.template field<true>(g, C, S, stage, p_own, gx, gy, zq);
+            if (out_plane) {
+                fb[zq % 3][ly + 1][lx + 1] = f_p;
+                if (has_halo) fb[zq % 3][hy][hx] = op.template field<true>(g, C, S, stage, p_halo, hgx, hgy, zq);
+            }
+        } else {
+            if (vxy) {
+                if (out_plane) o_p = op.template own<false>(g, C, S, stage, p_own, gx, gy, zq, f_p);
+                else f_p = op.template field<false>(g, C, S, stage, p_own, gx, gy, zq);
+            } else {
+                f_p = T(0);
+            }
+            if (out_plane) {
+                fb[zq % 3][ly + 1][lx + 1] = f_p;
+                if (has_halo) {
+                    T v = T(0);
+                    if (halo_in) v = op.template field<false>(g, C, S, stage, p_halo, hgx, hgy, zq);
+                    fb[zq % 3][hy][hx] = v;
+                }
+            }
+        }
+        __syncthreads();
+        if (s_err) break;
+        // Every thread is done with this stage: refill it with plane q+NSTAGE.
+        if (tid == 0 && q + NSTAGE < NP) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(q + NSTAGE);
+        }
+        const int zs = zq - 1;
+        if (zs >= z0 && zs < z1 && vxy) {
+            const T(*P)[HX] = fb[zs % 3];
+            const int64_t i = i_col + plane * zs;
+            if (blk_int && zs >= 1 && zs <= g.nz - 2)
+                op.template apply<true>(g, C, S, o_c, i, gx, gy, zs, f_c, P[ly + 1][lx + 2], P[ly + 1][lx],
+                                        P[ly + 2][lx + 1], P[ly][lx + 1], f_p, f_m);
+            else
+                op.template apply<false>(g, C, S, o_c, i, gx, gy, zs, f_c, P[ly + 1][lx + 2], P[ly + 1][lx],
+                                         P[ly + 2][lx + 1], P[ly][lx + 1], f_p, f_m);
+        }
+        f_m = f_c;
+        f_c = f_p;
+        o_c = o_p;
+    }
+
+    if (s_err) {
+        // Tile loads did not arrive in time.  Wait (bounded) for the copies
+        // this block issued and has not consumed, then fail the job.
+        if (tid == 0) {
+            const int issued = min(q + NSTAGE, NP);
+            for (int k = q; k < issued; ++k)
+                mbar_wait_bounded(smem_u32(&bars[k % NSTAGE]), (uint32_t)((k / NSTAGE) & 1));
+            atomicExch(&J.sc->state, (int32_t)FAULT);
+            atomicExch(&J.sc->outer_state, (int32_t)FAULT);
+        }
+        return;
+    }
+    // The last plane of the volume has no z+1 neighbour: apply it here.
+    if (pb == z1 - 1 && vxy) {
+        const int zs = z1 - 1;
+        const T(*P)[HX] = fb[zs % 3];
+        op.template apply<false>(g, C, S, o_c, i_col + plane * zs, gx, gy, zs, f_c, P[ly + 1][lx + 2],
+                                 P[ly + 1][lx], P[ly + 2][lx + 1], P[ly][lx + 1], T(0), f_m);
+    }
+
+    T v[NV];
+    op.partials(v);
+    block_sum_store<NV, T>(v, J.part + local * NPART, s_red);
+    if (arrive_last(J.counter, J.ntiles, &s_flag)) {
+        double tot[NV];
+        sum_partials<NV>(J.part, J.ntiles, tot, s_red);
+        if (tid == 0) {
+            Op::finish(*J.sc, tot);
+            *J.counter = 0u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Helpers shared by the ops.
+// ---------------------------------------------------------------------------
+struct NoShared {};
+
+// ===========================================================================
+// Setup of a pure-precision solve (F64 or F32): x = x0, r = b - A x0, and the
+// Krylov vectors zeroed.  Dots: |b|^2, |r|^2, r.z.
+// CG_Solve setup: CG.cu:38-63.  BICG_Solve setup: BICGSTAB.cu:49-91.
+// Streams: code.
+// ===========================================================================
+template <typename TT, typename ST, bool BICG>
+struct OpInit {
+    using T = TT;
+    using SL = Streams<1>;
+    static constexpr int NV = 3;
+    using Shared = NoShared;
+    struct Own { uint32_t code; };
+    const CUtensorMap *tmap[SL::N];
+    T *x, *r, *r0, *p0, *v0;
+    Acc<T> bb, rr, rz;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ void init(const Job &J, Shared &)
+    {
+        tmap[0] = &J.tm[TM_CODE];
+        x = (T *)J.x; r = (T *)J.r[0]; r0 = (T *)J.r0; p0 = (T *)J.p[0]; v0 = (T *)J.v[0];
+    }
+    template <bool INT>
+    __device__ T field(const Geo &g, const Coef<T> &, Shared &, const unsigned char *, const Pt &, int x_, int y_,
+                       int z_) const
+    {
+        return x0_at<T>(g, x_, y_, z_);
+    }
+    template <bool INT>
+    __device__ Own own(const Geo &g, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    {
+        f = x0_at<T>(g, x_, y_, z_);
+        return Own{(uint32_t)sv<uint8_t, SL, 0>(st, pt)};
+    }
+    template <bool INT>
+    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
+                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
+        const T ax = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T b = rhs_at<T>(C, g, o.code, x_, y_, z_);
+        const T res = b - ax;
+        x[i] = fc;
+        r[i] = res;
+        p0[i] = T(0);
+        if (BICG) {
+            r0[i] = res;
+            v0[i] = T(0);
+        }
+        const T inv = INT ? C.inv_int[o.code & 127] : (g.interior(x_, y_, z_) ? C.inv_int[o.code & 127] : T(1) / d);
+        bb.add_prod(b, b);
+        rr.add_prod(res, res);
+        rz.add_prod(res, res * inv);
+    }
+    __device__ void partials(T (&v)[NV]) const { v[0] = bb.hi(); v[1] = rr.hi(); v[2] = rz.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV])
+    {
+        const ST rhs = (ST)t[0];
+        sc.rhs_sq = rhs;
+        sc.iter = 0;
+        sc.restarts = 0;
+        sc.restart = 0;
+        if (rhs == ST(0)) {  // CG.cu:41-44, BICGSTAB.cu:66-69
+            sc.state = ZERO_RHS;
+            return;
+        }
+        const ST tol = (ST)sc.tol;
+        const ST tol2 = tol * tol * rhs;
+        sc.tol2 = tol2;
+        const ST rsq = (ST)t[1];
+        sc.rsq = rsq;
+        if (!BICG) {
+            sc.zr = (ST)t[2];
+            sc.beta = 0.0;
+        } else {
+            // First pass of the loop head: rho_old = 1, rho = r0.r = |r0|^2,
+            // alpha = w = 1, beta = (rho/rho_old)*(alpha/w) (BICGSTAB.cu:71-112).
+            sc.r0_sq = rsq;
+            sc.alpha = 1.0;
+            sc.omega = 1.0;
+            const ST rho = rsq;
+            sc.rho = rho;
+            sc.beta = (double)((rho / ST(1)) * (ST(1) / ST(1)));
+        }
+        if (!(rsq > tol2)) sc.state = CONVERGED;
+        else if (sc.max_iter == 0) sc.state = MAXITER;
+        else sc.state = RUNNING;
+    }
+};
+
+// ===========================================================================
+// CG step 1: p <- z + beta p (z = r/diag on the fly), q = A p, dot p.q.
+// CG.cu:113-135 (z, beta, p update of the previous iteration) + :70-81.
+// Streams: r, p_old, code.
+// ===========================================================================
+template <typename TT, typename ST>
+struct OpCG1 {
+    using T = TT;
+    using SL = Streams<sizeof(TT), sizeof(TT), 1>;
+    static constexpr int NV = 1;
+    using Shared = NoShared;
+    struct Own { uint32_t code; };
+    const CUtensorMap *tmap[SL::N];
+    T *pnew;
+    T beta;
+    Acc<T> pap;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ void init(const Job &J, Shared &)
+    {
+        const int par = (int)(J.sc->iter & 1);
+        tmap[0] = &J.tm[TM_R];
+        tmap[1] = &J.tm[TM_P + par];
+        tmap[2] = &J.tm[TM_CODE];
+        pnew = (T *)J.p[par ^ 1];
+        beta = (T)J.sc->beta;
+    }
+    template <bool INT>
+    __device__ __forceinline__ T pval(const Geo &g, const Coef<T> &C, const unsigned char *st, const Pt &pt,
+                                      int x_, int y_, int z_, uint32_t c) const
+    {
+        const T zi = sv<T, SL, 0>(st, pt) * inv_x<T, INT>(C, g, c, x_, y_, z_);
+        return sv<T, SL, 1>(st, pt) * beta + zi;  // __aAddAlphaBKernel: p = p*beta + z
+    }
+    template <bool INT>
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    {
+        return pval<INT>(g, C, st, pt, x_, y_, z_, sv<uint8_t, SL, 2>(st, pt));
+    }
+    template <bool INT>
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    {
+        const uint32_t c = sv<uint8_t, SL, 2>(st, pt);
+        f = pval<INT>(g, C, st, pt, x_, y_, z_, c);
+        return Own{c};
+    }
+    template <bool INT>
+    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
+                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
+        const T q = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        pnew[i] = fc;
+        pap.add_prod(fc, q);
+    }
+    __device__ void partials(T (&v)[NV]) const { v[0] = pap.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV])
+    {
+        sc.alpha = (double)((ST)sc.zr / (ST)t[0]);  // CG.cu:79-81
+    }
+};
+
+// ===========================================================================
+// CG step 2: q = A p (recomputed), x += alpha p, r -= alpha q, z = r/diag,
+// dots |r|^2 and r.z; convergence, beta and the iteration count.
+// CG.cu:87-154.  Streams: p, x, r, code.
+// ===========================================================================
+template <typename TT, typename ST>
+struct OpCG2 {
+    using T = TT;
+    using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), 1>;
+    static constexpr int NV = 2;
+    using Shared = NoShared;
+    struct Own { uint32_t code; T x, r; };
+    const CUtensorMap *tmap[SL::N];
+    T *x, *r;
+    T alpha;
+    Acc<T> rr, rz;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ void init(const Job &J, Shared &)
+    {
+        const int par = (int)(J.sc->iter & 1);
+        tmap[0] = &J.tm[TM_P + (par ^ 1)];
+        tmap[1] = &J.tm[TM_X];
+        tmap[2] = &J.tm[TM_R];
+        tmap[3] = &J.tm[TM_CODE];
+        x = (T *)J.x;
+        r = (T *)J.r[0];
+        alpha = (T)J.sc->alpha;
+    }
+    template <bool INT>
+    __device__ T field(const Geo &, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    {
+        return sv<T, SL, 0>(st, pt);
+    }
+    template <bool INT>
+    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    {
+        f = sv<T, SL, 0>(st, pt);
+        return Own{(uint32_t)sv<uint8_t, SL, 3>(st, pt), sv<T, SL, 1>(st, pt), sv<T, SL, 2>(st, pt)};
+    }
+    template <bool INT>
+    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
+                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
+        const T q = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T xn = o.x + alpha * fc;        // __aAddBetaBKernel(x, p, alpha)
+        const T rn = o.r + (-alpha) * q;      // __aAddBetaBKernel(r, ap, -alpha)
+        x[i] = xn;
+        r[i] = rn;
+        const T inv = INT ? C.inv_int[o.code & 127] : (g.interior(x_, y_, z_) ? C.inv_int[o.code & 127] : T(1) / d);
+        rr.add_prod(rn, rn);
+        rz.add_prod(rn, rn * inv);
+    }
+    __device__ void partials(T (&v)[NV]) const { v[0] = rr.hi(); v[1] = rz.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV])
+    {
+        const ST rsq = (ST)t[0];
+        sc.rsq = rsq;
+        if (rsq <= (ST)sc.tol2) {  // CG.cu:108-110: converging iteration not counted
+            sc.state = CONVERGED;
+            return;
+        }
+        const ST zr_new = (ST)t[1];
+        sc.beta = (double)(zr_new / (ST)sc.zr);  // CG.cu:121-123
+        sc.zr = zr_new;
+        sc.iter += 1;                            // CG.cu:144
+        if (sc.inner_mode) {
+            // FP32 inner solve: stop when the residual has grown far above
+            // its best value; the FP64 refinement decides what to keep.
+            if (rsq < (ST)sc.rsq_min) sc.rsq_min = rsq;
+            else if (rsq > (ST)1e4 * (ST)sc.rsq_min) { sc.state = STALLED; return; }
+        }
+        if (rsq > (ST)sc.div_thresh) sc.state = DIVERGED;  // CG.cu:152
+        else if (sc.iter >= sc.max_iter) sc.state = MAXITER;
+    }
+};
+
+// ===========================================================================
+// BiCGSTAB restart (BICGSTAB.cu:103-110): when |rho| < eps^2 |r0|^2 the
+// residual is recomputed from x and becomes the new shadow residual.  Runs
+// as a no-op kernel unless a restart is pending.  Streams: x, code.
+// ===========================================================================
+template <typename TT, typename ST>
+struct OpBiRestart {
+    using T = TT;
+    using SL = Streams<sizeof(TT), 1>;
+    static constexpr int NV = 1;
+    using Shared = NoShared;
+    struct Own { uint32_t code; };
+    const CUtensorMap *tmap[SL::N];
+    T *r, *r0;
+    Acc<T> rr;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING && sc.restart != 0; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ void init(const Job &J, Shared &)
+    {
+        const int par = (int)(J.sc->iter & 1);
+        tmap[0] = &J.tm[TM_X];
+        tmap[1] = &J.tm[TM_CODE];
+        r = (T *)J.r[par];
+        r0 = (T *)J.r0;
+    }
+    template <bool INT>
+    __device__ T field(const Geo &, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    {
+        return sv<T, SL, 0>(st, pt);
+    }
+    template <bool INT>
+    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    {
+        f = sv<T, SL, 0>(st, pt);
+        return Own{(uint32_t)sv<uint8_t, SL, 1>(st, pt)};
+    }
+    template <bool INT>
+    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
+                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
+        const T ax = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T res = rhs_at<T>(C, g, o.code, x_, y_, z_) - ax;
+        r[i] = res;
+        r0[i] = res;
+        rr.add_prod(res, res);
+    }
+    __device__ void partials(T (&v)[NV]) const { v[0] = rr.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV])
+    {
+        const ST rho = (ST)t[0];
+        sc.r0_sq = rho;
+        sc.rho = rho;
+        sc.restarts += 1;
+        sc.restart = 0;
+        const ST rho_old = (ST)sc.rho_old;
+        sc.beta = (double)((rho / rho_old) * ((ST)sc.alpha / (ST)sc.omega));
+    }
+};
+
+// ===========================================================================
+// BiCGSTAB step 1: p <- r + beta (p - w v), y = p/diag, v = A y, dot r0.v.
+// BICGSTAB.cu:112-147.  Streams: r, p_old, v_old, r0, code.
+// ===========================================================================
+template <typename TT, typename ST>
+struct OpBi1 {
+    using T = TT;
+    using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), sizeof(TT), 1>;
+    static constexpr int NV = 1;
+    using Shared = NoShared;
+    struct Own { uint32_t code; T p, r0; };
+    const CUtensorMap *tmap[SL::N];
+    T *pnew, *vnew;
+    T beta, nw;
+    Acc<T> r0v;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ void init(const Job &J, Shared &)
+    {
+        const int par = (int)(J.sc->iter & 1);
+        tmap[0] = &J.tm[TM_R + par];
+        tmap[1] = &J.tm[TM_P + par];
+        tmap[2] = &J.tm[TM_V + par];
+        tmap[3] = &J.tm[TM_R0];
+        tmap[4] = &J.tm[TM_CODE];
+        pnew = (T *)J.p[par ^ 1];
+        vnew = (T *)J.v[par ^ 1];
+        beta = (T)J.sc->beta;
+        nw = (T)(-J.sc->omega);
+    }
+    __device__ __forceinline__ T pval(const unsigned char *st, const Pt &pt) const
+    {
+        // __aPlusBetaBGammaPlusCKernel: p = beta*(p + (-w)*v) + r
+        return beta * (sv<T, SL, 1>(st, pt) + nw * sv<T, SL, 2>(st, pt)) + sv<T, SL, 0>(st, pt);
+    }
+    template <bool INT>
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    {
+        return pval(st, pt) * inv_x<T, INT>(C, g, sv<uint8_t, SL, 4>(st, pt), x_, y_, z_);
+    }
+    template <bool INT>
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    {
+        const uint32_t c = sv<uint8_t, SL, 4>(st, pt);
+        const T pn = pval(st, pt);
+        f = pn * inv_x<T, INT>(C, g, c, x_, y_, z_);
+        return Own{c, pn, sv<T, SL, 3>(st, pt)};
+    }
+    template <bool INT>
+    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
+                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
+        const T vn = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        pnew[i] = o.p;
+        vnew[i] = vn;
+        r0v.add_prod(o.r0, vn);
+    }
+    __device__ void partials(T (&v)[NV]) const { v[0] = r0v.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV])
+    {
+        sc.alpha = (double)((ST)sc.rho / (ST)t[0]);  // BICGSTAB.cu:147
+    }
+};
+
+// ===========================================================================
+// BiCGSTAB step 2: s = r - alpha v, z = s/diag, t = A z, dots t.s, t.t.
+// BICGSTAB.cu:149-183.  Streams: r, v_new, code.
+// ===========================================================================
+template <typename TT, typename ST>
+struct OpBi2 {
+    using T = TT;
+    using SL = Streams<sizeof(TT), sizeof(TT), 1>;
+    static constexpr int NV = 2;
+    using Shared = NoShared;
+    struct Own { uint32_t code; T s; };
+    const CUtensorMap *tmap[SL::N];
+    T nalpha;
+    Acc<T> ts, tt;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ void init(const Job &J, Shared &)
+    {
+        const int par = (int)(J.sc->iter & 1);
+        tmap[0] = &J.tm[TM_R + par];
+        tmap[1] = &J.tm[TM_V + (par ^ 1)];
+        tmap[2] = &J.tm[TM_CODE];
+        nalpha = (T)(-J.sc->alpha);
+    }
+    __device__ __forceinline__ T sval(const unsigned char *st, const Pt &pt) const
+    {
+        return sv<T, SL, 0>(st, pt) + nalpha * sv<T, SL, 1>(st, pt);  // s = r + (-alpha) v
+    }
+    template <bool INT>
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    {
+        return sval(st, pt) * inv_x<T, INT>(C, g, sv<uint8_t, SL, 2>(st, pt), x_, y_, z_);
+    }
+    template <bool INT>
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    {
+        const uint32_t c = sv<uint8_t, SL, 2>(st, pt);
+        const T s = sval(st, pt);
+        f = s * inv_x<T, INT>(C, g, c, x_, y_, z_);
+        return Own{c, s};
+    }
+    template <bool INT>
+    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t, int x_, int y_, int z_, T fc,
+                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
+        const T t = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        ts.add_prod(t, o.s);
+        tt.add_prod(t, t);
+    }
+    __device__ void partials(T (&v_)[NV]) const { v_[0] = ts.hi(); v_[1] = tt.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV])
+    {
+        const ST tmp = (ST)t[1];
+        sc.omega = (tmp > ST(0)) ? (double)((ST)t[0] / tmp) : 0.0;  // BICGSTAB.cu:175-183
+    }
+};
+
+// ===========================================================================
+// BiCGSTAB step 3: t recomputed, x += alpha y + w z, r = s - w t, dots r0.r and
+// |r|^2; divergence, iteration count, convergence, next rho/beta or a
+// restart.  BICGSTAB.cu:187-212 + the loop head :93-112.
+// Streams: r, v_new, p_new, x, r0, code.
+// ===========================================================================
+template <typename TT, typename ST>
+struct OpBi3 {
+    using T = TT;
+    using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), sizeof(TT), sizeof(TT), 1>;
+    static constexpr int NV = 2;
+    using Shared = NoShared;
+    struct Own { uint32_t code; T s, x, y, r0; };
+    const CUtensorMap *tmap[SL::N];
+    T *x, *rnew;
+    T alpha, omega, nalpha, nomega;
+    Acc<T> r0r, rr;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ void init(const Job &J, Shared &)
+    {
+        const int par = (int)(J.sc->iter & 1);
+        tmap[0] = &J.tm[TM_R + par];
+        tmap[1] = &J.tm[TM_V + (par ^ 1)];
+        tmap[2] = &J.tm[TM_P + (par ^ 1)];
+        tmap[3] = &J.tm[TM_X];
+        tmap[4] = &J.tm[TM_R0];
+        tmap[5] = &J.tm[TM_CODE];
+        x = (T *)J.x;
+        rnew = (T *)J.r[par ^ 1];
+        alpha = (T)J.sc->alpha;
+        omega = (T)J.sc->omega;
+        nalpha = -alpha;
+        nomega = -omega;
+    }
+    __device__ __forceinline__ T sval(const unsigned char *st, const Pt &pt) const
+    {
+        return sv<T, SL, 0>(st, pt) + nalpha * sv<T, SL, 1>(st, pt);
+    }
+    template <bool INT>
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    {
+        return sval(st, pt) * inv_x<T, INT>(C, g, sv<uint8_t, SL, 5>(st, pt), x_, y_, z_);
+    }
+    template <bool INT>
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    {
+        const uint32_t c = sv<uint8_t, SL, 5>(st, pt);
+        const T s = sval(st, pt);
+        const T inv = inv_x<T, INT>(C, g, c, x_, y_, z_);
+        f = s * inv;
+        return Own{c, s, sv<T, SL, 3>(st, pt), sv<T, SL, 2>(st, pt) * inv, sv<T, SL, 4>(st, pt)};
+    }
+    template <bool INT>
+    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
+                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
+        const T t = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        x[i] = o.x + (alpha * o.y + omega * fc);   // __ABC_BetaGammaKernel: x += a*y + w*z
+        const T rn = o.s + nomega * t;             // __aPlusBetaBKernel(s, t, r, -w)
+        rnew[i] = rn;
+        r0r.add_prod(o.r0, rn);
+        rr.add_prod(rn, rn);
+    }
+    __device__ void partials(T (&v_)[NV]) const { v_[0] = r0r.hi(); v_[1] = rr.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV])
+    {
+        const ST rsq = (ST)t[1];
+        sc.rsq = rsq;
+        if (rsq > (ST)sc.div_thresh) {  // BICGSTAB.cu:206-209, before ++i
+            sc.state = sc.inner_mode ? STALLED : DIVERGED;
+            return;
+        }
+        sc.iter += 1;  // BICGSTAB.cu:211
+        if (!(rsq > (ST)sc.tol2)) { sc.state = CONVERGED; return; }
+        if (sc.inner_mode) {
+            if (rsq < (ST)sc.rsq_min) sc.rsq_min = rsq;
+            else if (rsq > (ST)1e4 * (ST)sc.rsq_min) { sc.state = STALLED; return; }
+        }
+        if (sc.iter >= sc.max_iter) { sc.state = MAXITER; return; }
+        // Loop head of the next iteration (BICGSTAB.cu:95-112).
+        const ST rho_old = (ST)sc.rho;
+        const ST rho = (ST)t[0];
+        sc.rho_old = rho_old;
+        sc.rho = rho;
+        const ST mag = rho < ST(0) ? -rho : rho;
+        if (mag < (ST)sc.eps2 * (ST)sc.r0_sq) {
+            // A restart recomputes r = b - A x and takes it as the new shadow
+            // residual.  Inside a MIXED solve that is exactly the next FP64
+            // refinement step, so the inner solve ends here instead.
+            if (sc.inner_mode) sc.state = CONVERGED;
+            else sc.restart = 1;
+        } else {
+            sc.beta = (double)((rho / rho_old) * ((ST)sc.alpha / (ST)sc.omega));
+        }
+    }
+};
+
+}  // namespace ft

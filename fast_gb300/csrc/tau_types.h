@@ -1,0 +1,120 @@
+// Internal types shared by the host orchestration and the device kernels.
+#pragma once
+#include <cuda.h>
+#include <stdint.h>
+
+namespace ft {
+
+// Tile of one thread block: TX x TY columns marching over ZC planes in z.
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int NTHREADS = TX * TY;
+constexpr int HX = TX + 2;   // tile + 1-voxel halo
+constexpr int HY = TY + 2;
+constexpr int NPART = 4;     // partial sums per block per kernel
+
+// Stencil code byte: bit d (d = 0..5, Dir order X_POS, X_NEG, Y_POS, Y_NEG,
+// Z_POS, Z_NEG) = neighbour d is solid; bit 6 = the voxel itself is solid.
+// Out-of-domain neighbours repeat the voxel's own bit (the reference's
+// clamped neighbour, fastlib/src/solver/Diffusion.cpp:51-62).
+constexpr int SELF_BIT = 6;
+
+enum SolveState : int32_t {
+    RUNNING = 0,
+    CONVERGED = 1,
+    MAXITER = 2,
+    DIVERGED = 3,
+    ZERO_RHS = 4,
+    STALLED = 5,   // FP32 inner solve ended because its residual grew
+    FAULT = 6,     // a bounded device-side wait ran out (tile loads did not arrive)
+};
+
+// Tensor maps of a job's arrays (TMA descriptors), by array.
+enum TensorMapId : int {
+    TM_CODE = 0, TM_X = 1, TM_R = 2 /* +parity */, TM_R0 = 4, TM_P = 5 /* +parity */, TM_V = 7 /* +parity */,
+    TM_X64 = 9 /* +parity */, NTM = 11
+};
+
+// Per right-hand-side solver scalars, resident in device memory and updated
+// by the last block of each kernel ("finisher").
+struct Scalars {
+    double rhs_sq;      // |b|^2 of the system being iterated
+    double tol2;        // tol^2 |b|^2 (in solve precision)
+    double tol;         // relative tolerance of the system being iterated
+    double rsq;         // |r|^2 (recursive)
+    double zr;          // CG: r.z
+    double alpha, beta; // CG/BiCGSTAB
+    double rho, omega;  // BiCGSTAB
+    double rho_old;     // BiCGSTAB rho of the previous iteration (for a restart)
+    double r0_sq;       // BiCGSTAB |r0|^2
+    double div_thresh;  // divergence threshold on rsq (1e11 scaled to h=1 units)
+    double eps2;        // BiCGSTAB restart threshold eps(T)^2
+    uint64_t iter;      // iterations of the current (inner) solve, reference counting
+    uint64_t max_iter;  // iteration limit of the current (inner) solve
+    uint64_t restarts;
+    int32_t state;      // SolveState of the current (inner) solve
+    int32_t restart;    // BiCGSTAB: restart pending before the next iteration
+    // FP64 iterative refinement (MIXED)
+    double tol_outer;   // requested relative tolerance on the FP64 residual
+    double inner_floor; // smallest relative tolerance asked of one FP32 inner solve
+    double r64_sq;      // |b - A x64|^2
+    double b64_sq;      // |b|^2 in FP64
+    uint64_t total_iter;    // inner iterations summed over refinement steps
+    uint64_t max_total;     // limit on total_iter
+    int32_t outer_state;    // SolveState of the refinement loop
+    int32_t outer_steps;
+    int32_t x64_cur;        // which x64 buffer holds the current iterate
+    int32_t inner_mode;     // 1: FP32 inner solve of a MIXED solve
+    double rsq_min;         // smallest inner |r|^2 seen (growth guard)
+    int32_t rejects;        // refinement steps whose correction was rejected
+    int32_t reject_pending; // 1: the last correction was rejected; e must be zeroed and x64 re-evaluated
+    // reductions for tau and porosity
+    double flux_sum;    // sum over voxels of the tau flux term
+    uint64_t pores;     // number of zero (pore) voxels
+};
+
+// One right-hand side (a direction of a volume) inside a launch.  Arrays
+// are x-fastest with a row pitch of `pitch` elements (nx rounded up to 16) so
+// every row starts on a 16-byte boundary, as TMA requires.
+struct Job {
+    CUtensorMap tm[NTM];         // TMA descriptors of the arrays below
+    int32_t pitch;               // row pitch in elements (all arrays of the volume)
+    int32_t nx, ny, nz;
+    int32_t dir;                 // 0..5
+    int32_t tiles_x, tiles_y, tiles_z;
+    int32_t zc;                  // planes per block
+    int64_t tile_base;           // first block index of this job in the launch
+    int64_t ntiles;
+    const uint8_t *code;         // stencil codes, N bytes
+    const uint8_t *mask;         // raw mask (tau and porosity)
+    void *x;                     // solution (T); MIXED: FP32 correction e
+    void *r[2];                  // residual ping-pong (T)
+    void *r0;                    // BiCGSTAB shadow residual (T)
+    void *p[2];                  // search direction ping-pong (T)
+    void *v[2];                  // BiCGSTAB v ping-pong (T)
+    double *x64[2];              // MIXED FP64 solution ping-pong
+    Scalars *sc;
+    double *part;                // ntiles * NPART partial sums
+    uint32_t *counter;           // finisher arrival counter
+    // Coefficients in h = 1 units (the reference's values divided by the
+    // cell size h; tau and x are invariant to a common scale of A and b).
+    double dface[2][2];          // face coefficient by (self solid, neighbour solid)
+    double dcell[2];             // cell diffusivity by solid bit (pore, solid)
+    float fface[2][2];
+    float fdiag_int[128];        // interior diagonal by code (7 bits), FP32
+    float finv_int[128];         // 1/diag, FP32
+    double ddiag_int[128];       // interior diagonal, FP64
+    double dinv_int[128];        // 1/diag, FP64
+    float c_tau[2];              // tau cell coefficients (float coeffs of the reference)
+    int32_t inner_parity;        // unused, keeps alignment
+    int32_t pad0;
+};
+
+struct Launch {
+    Job *jobs;          // device array
+    int32_t njobs;
+    int32_t pad;
+    int64_t nblocks;    // total blocks = sum of job tiles
+};
+
+}  // namespace ft

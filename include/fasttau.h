@@ -1,0 +1,184 @@
+/*
+ * fasttau.h -- C ABI of the GB300 tortuosity engine (libfasttau.so).
+ *
+ * The drop-in boundary for fastlib's tortuosity path (krsvojte/fast):
+ *   template<T> T fast::getTortuosity(const Volume&, const TortuosityParams&,
+ *       DiffusionSolverType, Volume* concetrationOutput, size_t* iterationsOut)
+ *   (fastlib/include/fastlib/volume/VolumeMeasures.h:51-58, implemented at
+ *    fastlib/src/volume/VolumeMeasures.cpp:42-285)
+ * and its helpers getPorosity<T> (VolumeMeasures.h:60-61), getVolumeCCL
+ * (fastlib/src/volume/VolumeSegmentation.cpp:26-64).
+ *
+ * All entry points are plain C: pointers, sizes and POD structs.  Volumes are
+ * uint8 arrays with x fastest, index i = x + nx*(y + ny*z)
+ * (fastlib/include/fastlib/utility/Types.h:30-32); 0 = pore (D0), nonzero =
+ * solid (D1).  Every function returns a fast_status; on failure
+ * fast_last_error() gives a message for the calling thread.
+ */
+#ifndef FASTTAU_H
+#define FASTTAU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FAST_API __attribute__((visibility("default")))
+#else
+#define FAST_API
+#endif
+
+/* Status codes.  The reference reports every failure as tau = 0 plus a
+ * message on stderr (VolumeMeasures.cpp:50-58,100,104-125,157-159); the C
+ * ABI names the cause instead and the language shims map non-OK to 0. */
+typedef enum fast_status {
+    FAST_OK = 0,
+    FAST_BAD_TYPE = 1,      /* mask is not uint8 / bad argument (VolumeMeasures.cpp:50) */
+    FAST_NO_HOST_DATA = 2,  /* mask pointer is NULL (VolumeMeasures.cpp:55) */
+    FAST_NOMEM = 3,         /* device memory does not fit (VolumeMeasures.cpp:104-125) */
+    FAST_NO_CONVERGENCE = 4,/* iteration limit reached (CG.cpp:70, VolumeMeasures.cpp:157) */
+    FAST_DIVERGED = 5,      /* |r|^2 > 1e11 in reference units (CG.cu:152, BICGSTAB.cu:207) */
+    FAST_CUDA_ERROR = 6,    /* a CUDA call failed; the context stays usable */
+    FAST_TIMEOUT = 7,       /* a bounded device-side wait ran out */
+    FAST_BAD_ARG = 8        /* invalid dimension / direction / solver / precision */
+} fast_status;
+
+/* enum Dir (fastlib/include/fastlib/utility/PrimitiveTypes.h:142-150). */
+typedef enum fast_dir {
+    FAST_X_POS = 0, FAST_X_NEG = 1, FAST_Y_POS = 2,
+    FAST_Y_NEG = 3, FAST_Z_POS = 4, FAST_Z_NEG = 5
+} fast_dir;
+
+/* enum DiffusionSolverType (VolumeMeasures.h:15-18). */
+typedef enum fast_solver { FAST_SOLVER_BICGSTAB = 0, FAST_SOLVER_CG = 1 } fast_solver;
+
+/* Arithmetic of the solve.  F64 / F32 are the reference's `-p double` /
+ * `-p float` (TauModule.h:19,125-129): the whole solve in that type.  MIXED is
+ * the engine's fast path: FP32 inner iterations with compensated dot
+ * products inside an FP64 iterative-refinement loop whose true residual
+ * b - A x, correction update of x and tau integral are FP64. */
+typedef enum fast_precision { FAST_PREC_F64 = 0, FAST_PREC_F32 = 1, FAST_PREC_MIXED = 2 } fast_precision;
+
+/* Face diffusivity between two voxels.  The reference uses the arithmetic
+ * mean (fastlib/src/cuda/Diffusion.cu:47-53, fastlib/src/solver/Diffusion.cpp:
+ * 119-125); HARMONIC is an opt-in extension and never the parity mode. */
+typedef enum fast_face_mean { FAST_FACE_ARITHMETIC = 0, FAST_FACE_HARMONIC = 1 } fast_face_mean;
+
+/* TortuosityParams (VolumeMeasures.h:20-34) + the CLI's precision/solver. */
+typedef struct fast_tau_params {
+    int32_t dir;            /* fast_dir; reference default X_NEG */
+    int32_t solver;         /* fast_solver; reference API default BICGSTAB, CLI default CG */
+    int32_t precision;      /* fast_precision */
+    int32_t face_mean;      /* fast_face_mean; 0 = arithmetic */
+    double tolerance;       /* relative residual, reference default 1e-6 */
+    uint64_t max_iter;      /* reference default 10000; MIXED: cap on total inner iterations */
+    double d0;              /* pore diffusivity; the reference passes float 1.0 */
+    double d1;              /* solid diffusivity; the reference passes (double)0.001f */
+    double porosity;        /* < 0: computed on the GPU (getPorosity<T>); else used as given */
+    int32_t verbose;        /* print per-solve summary to stderr */
+    int32_t flags;          /* FAST_FLAG_* */
+} fast_tau_params;
+
+/* fast_tau_params.flags: time every kernel launch of the solve with CUDA
+ * events (launches are serialised and not graph-replayed while profiling). */
+#define FAST_FLAG_PROFILE 1
+
+/* Per-direction result. */
+typedef struct fast_tau_result {
+    double tau;             /* 0 on failure, as the reference */
+    double porosity;        /* the porosity used */
+    double rel_residual;    /* |r|/|b| at exit (recursive residual; MIXED: true FP64 residual) */
+    uint64_t iterations;    /* reference counting: CG excludes the converging iteration,
+                               BiCGSTAB counts it (CG.cu:109-144, BICGSTAB.cu:211);
+                               MIXED: total inner iterations over all refinement steps */
+    uint32_t outer_steps;   /* MIXED: refinement steps (0 otherwise) */
+    int32_t status;         /* fast_status */
+} fast_tau_result;
+
+/* Fill *p with the reference defaults (TortuosityParams with the CLI's
+ * float coeffs {1.0, 0.001}): dir X_NEG, BICGSTAB, F64, tol 1e-6, 10000 iters. */
+FAST_API void fast_tau_params_init(fast_tau_params *p);
+
+/* getTortuosity<T> (VolumeMeasures.h:51-58).  `mask` is a HOST uint8 array of
+ * nx*ny*nz voxels, borrowed.  Solves one direction on the calling thread's
+ * device and stream, synchronously.  conc_out (nullable) receives the HOST
+ * concentration field: double for F64/MIXED, float for F32 (the reference's
+ * concetrationOutput, VolumeMeasures.cpp:146-149).  tau/iters/rel_err are
+ * nullable.  Returns FAST_OK or the failure cause; *tau is 0 on failure. */
+FAST_API int fast_tau_solve(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz,
+                            const fast_tau_params *p, double *tau, uint64_t *iters,
+                            double *rel_err, void *conc_out);
+
+/* Several directions of one volume in one call: the directions share the
+ * device-resident phase field and are advanced together as multiple
+ * right-hand sides (one launch per kernel step for all of them).  `dirs` has
+ * ndirs entries (each a fast_dir, ndirs <= 6); p->dir is ignored.  results has
+ * ndirs entries.  Returns the first non-OK status, FAST_OK if all succeeded. */
+FAST_API int fast_tau_solve_dirs(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz,
+                                 const fast_tau_params *p, int32_t ndirs, const int32_t *dirs,
+                                 fast_tau_result *results);
+
+/* The same on a DEVICE-resident mask (a cudaMalloc'ed pointer on the current
+ * device) on a caller stream (cudaStream_t passed as void*, NULL = the
+ * library's stream).  Synchronises that stream before returning. */
+FAST_API int fast_tau_solve_dirs_device(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz,
+                                        const fast_tau_params *p, int32_t ndirs,
+                                        const int32_t *dirs, fast_tau_result *results,
+                                        void *stream);
+
+/* getPorosity<T> (VolumeMeasures.h:60-61 via Volume::sumZeroElems,
+ * fastlib/src/volume/Volume.cpp:261-272): fraction of zero voxels, counted on
+ * the GPU.  pore_count is nullable. */
+FAST_API int fast_porosity(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz,
+                           double *porosity, uint64_t *pore_count);
+
+/* Kernel kinds of fast_tau_stats. */
+enum {
+    FAST_K_CODE = 0, FAST_K_INIT = 1, FAST_K_CG1 = 2, FAST_K_CG2 = 3, FAST_K_BI_RESTART = 4,
+    FAST_K_BI1 = 5, FAST_K_BI2 = 6, FAST_K_BI3 = 7, FAST_K_REFINE = 8, FAST_K_INIT64 = 9,
+    FAST_K_TAU = 10, FAST_K_COUNT = 16
+};
+
+/* Launch statistics of the calling thread's last solve. */
+typedef struct fast_tau_stats {
+    uint64_t launches;                 /* kernel launches of the engine (graph-replayed ones included) */
+    uint64_t graph_replays;
+    uint64_t kernel_launches[FAST_K_COUNT];
+    double kernel_ms[FAST_K_COUNT];    /* summed CUDA-event durations (FAST_FLAG_PROFILE only) */
+    int32_t profiled;
+    int32_t pad;
+} fast_tau_stats;
+
+FAST_API int fast_tau_last_stats(fast_tau_stats *out);
+
+/* Message of the calling thread's last failure ("" if none). */
+FAST_API const char *fast_last_error(void);
+
+/* Library version string. */
+FAST_API const char *fast_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Synthetic microstructures (the reference's VolumeGenerator uses an        */
+/* unseedable process-global RNG, VolumeGenerator.cpp:14; these generators   */
+/* are seeded and bit-identical across hosts).  255 = solid, 0 = pore        */
+/* (VolumeGenerator.cpp:218).  Output is a host array of nx*ny*nz bytes.      */
+/* ------------------------------------------------------------------------ */
+
+/* Overlapping solid spheres of radius uniform in [r_min, r_max] voxels added
+ * until the solid fraction reaches `solid_fraction`. */
+FAST_API int fast_gen_spheres(uint8_t *out, int64_t nx, int64_t ny, int64_t nz, uint64_t seed,
+                              double r_min, double r_max, double solid_fraction);
+
+/* Randomly oriented solid ellipsoids (uniform random rotations) with
+ * semi-axes (a, a*aspect, a*aspect), overlapping allowed, added until the
+ * solid fraction is reached (stand-in for the reference's SA packer). */
+FAST_API int fast_gen_ellipsoids(uint8_t *out, int64_t nx, int64_t ny, int64_t nz, uint64_t seed,
+                                 double semi_major, double aspect, double solid_fraction);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FASTTAU_H */
