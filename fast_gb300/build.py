@@ -50,7 +50,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
-    common = ["-O3", "-std=c++17", "-I", INCLUDE, "-I", CSRC]
+    common = ["-O3", "-std=c++17", "-I", INCLUDE, "-I", CSRC] + os.environ.get("FAST_TAU_NVCC_FLAGS", "").split()
     procs, objs = [], []
     for src in CUDA_SOURCES:
         obj = os.path.join(OUT, src.replace(".cu", ".o"))

@@ -5,7 +5,11 @@
 
 namespace ft {
 
-constexpr int kStages = 4;
+#ifndef FAST_TAU_STAGES_F32
+#define FAST_TAU_STAGES_F32 4
+#endif
+// Depth of the TMA stage ring (planes of every operand in flight per block).
+constexpr int kStages = FAST_TAU_STAGES_F32;
 
 template <class Op>
 static void go(const Launch &L, cudaStream_t st)

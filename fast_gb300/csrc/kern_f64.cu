@@ -4,7 +4,11 @@
 
 namespace ft {
 
-constexpr int kStages = 3;
+#ifndef FAST_TAU_STAGES_F64
+#define FAST_TAU_STAGES_F64 3
+#endif
+// Depth of the TMA stage ring (planes of every operand in flight per block).
+constexpr int kStages = FAST_TAU_STAGES_F64;
 
 template <class Op>
 static void go(const Launch &L, cudaStream_t st)

@@ -290,6 +290,26 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
 {
     cudaStream_t st = E.stream;
     const int chunk = std::max(1, env_int("FAST_TAU_CHUNK", 16));
+    if (env_int("FAST_TAU_TRACE", 0) >= 2) {
+        // Trace: direct launches, scalars of job 0 printed after each kernel.
+        for (uint64_t it = 0; it < max_iter + 2; it++) {
+            bool running = false;
+            for (Step s : steps) {
+                launch(s, L, st);
+                CU(cudaMemcpyAsync(E.h_sc, d_sc, sizeof(Scalars) * njobs, cudaMemcpyDeviceToHost, st));
+                CU(cudaStreamSynchronize(st));
+                const Scalars &S = E.h_sc[0];
+                fprintf(stderr,
+                        "trace step %d iter %llu state %d rsq %.6e zr %.6e alpha %.6e beta %.6e rho %.6e omega %.6e "
+                        "dots %.6e %.6e %.6e\n",
+                        (int)s, (unsigned long long)S.iter, S.state, S.rsq, S.zr, S.alpha, S.beta, S.rho, S.omega,
+                        S.dbg[0], S.dbg[1], S.dbg[2]);
+            }
+            for (int j = 0; j < njobs; j++) running |= (E.h_sc[j].state == RUNNING);
+            if (!running) break;
+        }
+        return FAST_OK;
+    }
     if (t_prof.on) {
         // Profiling: direct launches, each timed; the scalars are read after
         // every chunk.
@@ -519,6 +539,13 @@ int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64
             for (int j = 0; j < ndirs; j++) {
                 running |= hs[j].outer_state == RUNNING;
                 inner |= hs[j].state == RUNNING;
+                if (env_int("FAST_TAU_TRACE", 0))
+                    fprintf(stderr,
+                            "trace refine %d job %d outer_state %d state %d relres64 %.3e inner_tol %.3e total_iter %llu "
+                            "rejects %d pending %d\n",
+                            o, j, hs[j].outer_state, hs[j].state,
+                            hs[j].b64_sq > 0 ? std::sqrt(hs[j].r64_sq / hs[j].b64_sq) : 0.0, hs[j].tol,
+                            (unsigned long long)hs[j].total_iter, hs[j].rejects, hs[j].reject_pending);
             }
             if (!running) break;
             // e = 0 for the next inner solve, and for a rejected correction.

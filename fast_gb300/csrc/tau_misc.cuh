@@ -85,14 +85,23 @@ struct OpRefine {
         if (t[1] == 0.0) { sc.outer_state = ZERO_RHS; return; }
         // Keep a correction only if it lowered the true FP64 residual.  A
         // rejected one leaves x64 as it was; the host zeroes e and this step
-        // runs again, which re-evaluates x64 and restarts the inner solve
-        // from its true residual (a fresh shadow residual for BiCGSTAB).
+        // runs again, which re-evaluates x64 and sets up the same inner solve
+        // bit for bit (every reduction has a fixed order).  That replay stops
+        // at the iteration where the rejected solve had its smallest
+        // residual, so it returns the best correction the solve passed by.
         if (sc.outer_steps > 0 && !sc.reject_pending && !(t[0] < sc.r64_sq)) {
             sc.rejects += 1;
-            if (sc.rejects > 8 || sc.total_iter >= sc.max_total) { sc.outer_state = MAXITER; return; }
+            const uint64_t best = sc.iter_min;
+            if (best == 0 || sc.replay_iters != 0 || sc.rejects > 8 || sc.total_iter >= sc.max_total) {
+                sc.outer_state = MAXITER;
+                return;
+            }
+            sc.replay_iters = best;
             sc.reject_pending = 1;
             return;
         }
+        const uint64_t replay = sc.reject_pending ? sc.replay_iters : 0;
+        if (!sc.reject_pending) sc.replay_iters = 0;
         sc.reject_pending = 0;
         sc.x64_cur ^= 1;
         sc.r64_sq = t[0];
@@ -121,7 +130,9 @@ struct OpRefine {
         sc.restarts = 0;
         sc.restart = 0;
         sc.max_iter = sc.max_total - sc.total_iter;
+        if (replay != 0 && replay < sc.max_iter) sc.max_iter = replay;
         sc.rsq_min = t[2];
+        sc.iter_min = 0;
         sc.outer_steps += 1;
         sc.state = (t[2] > sc.tol2) ? RUNNING : CONVERGED;
     }

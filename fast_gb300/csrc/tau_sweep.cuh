@@ -150,7 +150,7 @@ template <typename T, bool INT>
 __device__ __forceinline__ T inv_x(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
 {
     if constexpr (INT) return C.inv_int[code & 127];
-    else return inv_x<T, INT>(C, g, code, x, y, z);
+    else return inv_diag_at<T>(C, g, code, x, y, z);
 }
 template <typename T, bool INT>
 __device__ __forceinline__ T stencil_x(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z, T fc,
@@ -357,6 +357,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
         double tot[NV];
         sum_partials<NV>(J.part, J.ntiles, tot, s_red);
         if (tid == 0) {
+            for (int k = 0; k < NV && k < 4; k++) J.sc->dbg[k] = tot[k];
             Op::finish(*J.sc, tot);
             *J.counter = 0u;
         }
@@ -592,10 +593,11 @@ struct OpCG2 {
         sc.zr = zr_new;
         sc.iter += 1;                            // CG.cu:144
         if (sc.inner_mode) {
-            // FP32 inner solve: stop when the residual has grown far above
-            // its best value; the FP64 refinement decides what to keep.
-            if (rsq < (ST)sc.rsq_min) sc.rsq_min = rsq;
-            else if (rsq > (ST)1e4 * (ST)sc.rsq_min) { sc.state = STALLED; return; }
+            // FP32 inner solve: remember the best iterate and stop once the
+            // residual has grown well above it; the FP64 refinement decides
+            // what to keep.
+            if (rsq < (ST)sc.rsq_min) { sc.rsq_min = rsq; sc.iter_min = sc.iter; }
+            else if (rsq > (ST)100 * (ST)sc.rsq_min) { sc.state = STALLED; return; }
         }
         if (rsq > (ST)sc.div_thresh) sc.state = DIVERGED;  // CG.cu:152
         else if (sc.iter >= sc.max_iter) sc.state = MAXITER;
@@ -866,8 +868,8 @@ struct OpBi3 {
         sc.iter += 1;  // BICGSTAB.cu:211
         if (!(rsq > (ST)sc.tol2)) { sc.state = CONVERGED; return; }
         if (sc.inner_mode) {
-            if (rsq < (ST)sc.rsq_min) sc.rsq_min = rsq;
-            else if (rsq > (ST)1e4 * (ST)sc.rsq_min) { sc.state = STALLED; return; }
+            if (rsq < (ST)sc.rsq_min) { sc.rsq_min = rsq; sc.iter_min = sc.iter; }
+            else if (rsq > (ST)100 * (ST)sc.rsq_min) { sc.state = STALLED; return; }
         }
         if (sc.iter >= sc.max_iter) { sc.state = MAXITER; return; }
         // Loop head of the next iteration (BICGSTAB.cu:95-112).

@@ -66,11 +66,14 @@ struct Scalars {
     int32_t x64_cur;        // which x64 buffer holds the current iterate
     int32_t inner_mode;     // 1: FP32 inner solve of a MIXED solve
     double rsq_min;         // smallest inner |r|^2 seen (growth guard)
+    uint64_t iter_min;      // inner iterations completed when rsq_min was reached
+    uint64_t replay_iters;  // >0: stop the next inner solve after this many iterations
     int32_t rejects;        // refinement steps whose correction was rejected
     int32_t reject_pending; // 1: the last correction was rejected; e must be zeroed and x64 re-evaluated
     // reductions for tau and porosity
     double flux_sum;    // sum over voxels of the tau flux term
     uint64_t pores;     // number of zero (pore) voxels
+    double dbg[4];      // the last kernel's reduced dot products (tracing)
 };
 
 // One right-hand side (a direction of a volume) inside a launch.  Arrays
