@@ -1,0 +1,188 @@
+"""CPU tests of the oracle (the reference restatement the CUDA path is
+checked against): closed-form known answers of the reference discretisation,
+the committed golden fixtures, an independent scipy assembly + direct solve,
+symmetry properties, porosity and 6-connected labels."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+D1 = float(np.float32(0.001))
+
+
+def rel(a, b):
+    return abs(a - b) / abs(b)
+
+
+def test_all_pore_tau_is_one(oracle):
+    m = np.zeros((5, 6, 7), np.uint8)
+    for d in range(6):
+        for s in (oracle.CG, oracle.BICGSTAB):
+            r = oracle.get_tortuosity(m, dir=d, solver=s, tol=1e-12)
+            assert r["status"] == 0
+            assert abs(r["tau"] - 1.0) < 1e-9
+
+
+def test_all_pore_profile_is_linear(oracle):
+    # c_i = 1 - (i + 1/2)/n along the axis for a positive direction
+    m = np.zeros((3, 4, 10), np.uint8)
+    r = oracle.get_tortuosity(m, dir=oracle.X_POS, solver=oracle.CG, tol=1e-13, return_conc=True)
+    c = r["conc"][1, 2, :]
+    assert np.allclose(c, 1 - (np.arange(10) + 0.5) / 10, atol=1e-10)
+
+
+def test_all_solid_tau_is_zero(oracle):
+    m = np.full((4, 4, 4), 255, np.uint8)
+    r = oracle.get_tortuosity(m, dir=oracle.X_POS, solver=oracle.CG, tol=1e-10)
+    assert r["status"] == 0 and r["tau"] == 0.0
+
+
+@pytest.mark.parametrize("d", [0, 1])
+def test_parallel_layers(oracle, d):
+    """Pore/solid layers parallel to the axis: tau = phi / (phi + (1-phi) D1)."""
+    m = np.zeros((6, 8, 12), np.uint8)
+    m[:, 2:5, :] = 255
+    phi = (m == 0).mean()
+    r = oracle.get_tortuosity(m, dir=d, solver=oracle.CG, tol=1e-13)
+    assert rel(r["tau"], phi / (phi + (1 - phi) * D1)) < 1e-10
+
+
+def test_series_layers_arithmetic_mean(oracle):
+    """Layers in series along x: the 1-D resistor chain with ARITHMETIC face
+    diffusivity (the reference's choice, Diffusion.cu:47-53).  The harmonic
+    mean would give a different tau; this pins which mean is implemented."""
+    n = 9
+    solid = np.array([0, 0, 1, 1, 0, 1, 0, 0, 1], bool)
+    m = np.zeros((2, 3, n), np.uint8)
+    m[:, :, solid] = 255
+    D = np.where(solid, D1, 1.0)
+    # resistances in h = 1 units: half cell at both Dirichlet faces, faces between
+    R = 1 / (2 * D[0]) + sum(2 / (D[i] + D[i + 1]) for i in range(n - 1)) + 1 / (2 * D[-1])
+    J = 1.0 / R
+    # concentrations and the reference's cell-D flux terms
+    c = [1 - J / (2 * D[0])]
+    for i in range(n - 1):
+        c.append(c[-1] - J * 2 / (D[i] + D[i + 1]))
+    f = [D[i] * (c[i] - c[i + 1]) for i in range(n - 1)] + [D[-1] * c[-1] / 0.5]
+    phi = (~solid).mean()
+    tau_expected = phi / sum(f)
+    r = oracle.get_tortuosity(m, dir=oracle.X_POS, solver=oracle.CG, tol=1e-13)
+    assert rel(r["tau"], tau_expected) < 1e-9
+    # the harmonic-mean operator differs by far more than the tolerance
+    Rh = 1 / (2 * D[0]) + sum((D[i] + D[i + 1]) / (2 * D[i] * D[i + 1]) for i in range(n - 1)) + 1 / (2 * D[-1])
+    assert abs(Rh - R) / R > 1e-2
+
+
+def test_direction_mirror_symmetry(oracle, ):
+    rng = np.random.default_rng(3)
+    m = ((rng.random((6, 7, 9)) < 0.4) * 255).astype(np.uint8)
+    a = oracle.get_tortuosity(m, dir=oracle.X_POS, solver=oracle.CG, tol=1e-13)["tau"]
+    b = oracle.get_tortuosity(np.ascontiguousarray(m[:, :, ::-1]), dir=oracle.X_NEG, solver=oracle.CG, tol=1e-13)["tau"]
+    assert rel(a, b) < 1e-9
+
+
+def test_axis_transpose_symmetry(oracle):
+    rng = np.random.default_rng(4)
+    m = ((rng.random((6, 7, 9)) < 0.4) * 255).astype(np.uint8)
+    tx = oracle.get_tortuosity(m, dir=oracle.X_POS, solver=oracle.CG, tol=1e-13)["tau"]
+    # swap x and y: array [z, y, x] -> [z, x, y]
+    mt = np.ascontiguousarray(np.transpose(m, (0, 2, 1)))
+    ty = oracle.get_tortuosity(mt, dir=oracle.Y_POS, solver=oracle.CG, tol=1e-13)["tau"]
+    assert rel(tx, ty) < 1e-9
+
+
+def test_stored_system_spmv_matches_dense(oracle):
+    rng = np.random.default_rng(5)
+    m = ((rng.random((3, 4, 5)) < 0.5) * 255).astype(np.uint8)
+    A, b, x0 = oracle.assemble(m, oracle.Y_NEG)
+    N = m.size
+    nz, ny, nx = m.shape
+    dense = np.zeros((N, N))
+    off = {0: 1, 1: -1, 2: nx, 3: -nx, 4: nx * ny, 5: -nx * ny}
+    for d in range(6):
+        for i in range(N):
+            if A[d, i] != 0:
+                dense[i, i + off[d]] = A[d, i]
+    dense[np.arange(N), np.arange(N)] = A[6]
+    x = rng.random(N)
+    assert np.allclose(oracle.spmv(A, m.shape, x), dense @ x, rtol=1e-13, atol=0)
+    assert np.allclose(dense, dense.T)  # the operator is symmetric
+
+
+def _case_volume(c, volumes):
+    shape = tuple(c["shape"])
+    if c["kind"] == "spheres":
+        return volumes.spheres(shape, c["seed"], c["r"], c["r"], c["frac"])
+    if c["kind"] == "ellipsoids":
+        return volumes.ellipsoids(shape, c["seed"], c["r"], 0.35, 0.55)
+    return np.array(c["volume"], np.uint8).reshape(shape)
+
+
+def test_golden_small_cases(oracle, native):
+    """The oracle reproduces the committed fixtures exactly (same host
+    arithmetic, fixed reduction order), and agrees with the independent
+    scipy direct solve to the solver tolerance."""
+    from fast_gb300 import volumes
+    with open(os.path.join(GOLDEN, "small_cases.json")) as f:
+        cases = json.load(f)["cases"]
+    for c in cases:
+        m = _case_volume(c, volumes)
+        assert hashlib.sha256(m.tobytes()).hexdigest() == c["sha256"], "generator changed"
+        assert oracle.count_pores(m) == c["pores"]
+        for e in c["results"][:3]:
+            d = e["dir"]
+            for key, (s, v) in {"cg_device_1e-10": (oracle.CG, oracle.DEVICE),
+                                "bicgstab_eigen_1e-06": (oracle.BICGSTAB, oracle.EIGEN)}.items():
+                tol = float(key.rsplit("_", 1)[1])
+                r = oracle.get_tortuosity(m, dir=d, solver=s, tol=tol, variant=v)
+                tau, it, st = e[key]
+                assert r["status"] == st and r["iters"] == it
+                assert rel(r["tau"], tau) < 1e-12 if tau else r["tau"] == 0
+            if e["scipy_tau"]:
+                assert rel(e["cg_device_1e-10"][0], e["scipy_tau"]) < 1e-8
+
+
+def test_golden_workload_fixture_consistent():
+    with open(os.path.join(GOLDEN, "workloads.json")) as f:
+        w = json.load(f)["workloads"]
+    e = w["ellipsoids256"]
+    for d, r in e["dirs"].items():
+        # CG and BiCGSTAB driven to 1e-10 agree on tau far below 1e-5
+        assert rel(r["tau_cg_1e-10"], r["tau_bicgstab_eigen_1e-10"]) < 1e-8
+
+
+def test_porosity_count(oracle):
+    rng = np.random.default_rng(6)
+    m = ((rng.random((7, 8, 9)) < 0.3) * 255).astype(np.uint8)
+    assert oracle.count_pores(m) == int((m == 0).sum())
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_ccl_matches_scipy_label(oracle, seed):
+    """Labels numbered by minimum linear index == scipy.ndimage.label in raster
+    order with 6-connectivity on an [z, y, x] array."""
+    ndi = pytest.importorskip("scipy.ndimage")
+    rng = np.random.default_rng(seed)
+    m = ((rng.random((12, 13, 14)) < 0.55) * 255).astype(np.uint8)
+    labels, n = oracle.ccl_label(m, background=255)
+    ref, k = ndi.label(m != 255, structure=ndi.generate_binary_structure(3, 1))
+    assert n == k + 1
+    assert np.array_equal(labels, ref.astype(np.uint32))
+
+
+def test_ccl_boundary_table(oracle):
+    m = np.full((4, 5, 6), 255, np.uint8)
+    m[1:3, 2, :] = 0      # spans x from face X_NEG to X_POS
+    m[0, 0, 0] = 0        # corner voxel: X_NEG, Y_NEG, Z_NEG faces
+    labels, n = oracle.ccl_label(m, background=255)
+    assert n == 3
+    b = oracle.ccl_boundary(labels, n)
+    corner, bar = labels[0, 0, 0], labels[1, 2, 3]
+    assert b[1, corner] and b[3, corner] and b[5, corner] and not b[0, corner]
+    assert b[0, bar] and b[1, bar] and not b[2, bar]
+    assert not b[6].any()  # no label touches all six faces
