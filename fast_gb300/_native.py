@@ -55,6 +55,8 @@ SIGNATURES = {
     "fast_porosity": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_double),
                                 C.POINTER(C.c_uint64)]),
     "fast_tau_last_stats": (C.c_int, [C.POINTER(fast_tau_stats)]),
+    "fast_porosity_device_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_uint64),
+                                               C.POINTER(C.c_double), C.c_void_p]),
     "fast_last_error": (C.c_char_p, []),
     "fast_version": (C.c_char_p, []),
     "fast_gen_spheres": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_double,

@@ -45,6 +45,19 @@ static int fail(int status, const char *fmt, ...)
     return status;
 }
 
+int ft_fail(int status, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+void ft_clear_error() { g_last_error.clear(); }
+
 #define CU(call)                                                                                   \
     do {                                                                                           \
         cudaError_t e_ = (call);                                                                   \

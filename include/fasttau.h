@@ -154,6 +154,20 @@ typedef struct fast_tau_stats {
 
 FAST_API int fast_tau_last_stats(fast_tau_stats *out);
 
+/* Pore count of a DEVICE-resident mask that allocates nothing, for callers
+ * that cannot allocate device memory: code running while a stream is being
+ * captured into a CUDA graph, or an application whose device memory is owned
+ * by its own allocator.  No counterpart in the reference.  The reduction's
+ * scratch is a 256 KiB static device array inside the library, held by every
+ * GPU that loads the library until exit; volumes above 2,145,386,496 voxels
+ * (32736 blocks x 65536 voxels) are rejected with FAST_BAD_ARG.  The first
+ * call on a device looks up the array's device address: make it before any
+ * stream capture.  All calls share the array, so calls that overlap on the
+ * GPU race.  stream: a cudaStream_t as void*, NULL = the legacy default
+ * stream; the call synchronises it.  porosity is nullable. */
+FAST_API int fast_porosity_device_noalloc(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz,
+                                          uint64_t *pore_count, double *porosity, void *stream);
+
 /* Message of the calling thread's last failure ("" if none). */
 FAST_API const char *fast_last_error(void);
 
