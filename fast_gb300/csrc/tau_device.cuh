@@ -85,18 +85,21 @@ __device__ __forceinline__ T diag_general(const Coef<T> &C, const Geo &g, uint32
     return d;
 }
 
+// Diagonal and its inverse: table lookups for a voxel with all six
+// neighbours inside the domain, the coordinate-aware evaluation for a voxel
+// on a domain face (BND_BIT of its code).
 template <typename T>
-__device__ __forceinline__ T diag_at(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+__device__ __forceinline__ T diag_of(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
 {
-    if (g.interior(x, y, z)) return C.diag_int[code & 127];
-    return diag_general(C, g, code, x, y, z);
+    if (code & (1u << BND_BIT)) return diag_general(C, g, code, x, y, z);
+    return C.diag_int[code & 127];
 }
 
 template <typename T>
-__device__ __forceinline__ T inv_diag_at(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+__device__ __forceinline__ T inv_of(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
 {
-    if (g.interior(x, y, z)) return C.inv_int[code & 127];
-    return T(1) / diag_general(C, g, code, x, y, z);
+    if (code & (1u << BND_BIT)) return T(1) / diag_general(C, g, code, x, y, z);
+    return C.inv_int[code & 127];
 }
 
 // Right-hand side b (Diffusion.cuh:108-122): on the first plane of the
@@ -122,23 +125,24 @@ __device__ __forceinline__ T x0_at(const Geo &g, int x, int y, int z)
     return (g.sgn > 0) ? (T(1.0f) - q) : q;
 }
 
-// y = A f at (x,y,z) given the field at the voxel and its 6 neighbours, in
+// y = A f at a voxel given the field at the voxel and its 6 neighbours, in
 // the reference's summation order X+,X-,Y+,Y-,Z+,Z-,diag
-// (LinearSystemDevice.cuh:67-80); faces to out-of-domain neighbours have a
-// zero (skipped) coefficient.
+// (LinearSystemDevice.cuh:67-80).  A neighbour outside the domain carries a
+// field value of exactly 0 (the sweep writes 0 there), which drops its term
+// just as the reference's zeroed boundary coefficient does; no bounds test is
+// needed.
 template <typename T>
-__device__ __forceinline__ T apply_stencil(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z,
-                                           T fc, T fxp, T fxm, T fyp, T fym, T fzp, T fzm, T diag)
+__device__ __forceinline__ T stencil7(const Coef<T> &C, uint32_t code, T fc, T fxp, T fxm, T fyp, T fym, T fzp,
+                                      T fzm, T diag)
 {
     const int self = (code >> SELF_BIT) & 1;
     const T a = C.face[self][0], b = C.face[self][1];
-    T s = T(0);
-    if (x + 1 < g.nx) s += fxp * ((code & 1) ? b : a);
-    if (x > 0)        s += fxm * ((code & 2) ? b : a);
-    if (y + 1 < g.ny) s += fyp * ((code & 4) ? b : a);
-    if (y > 0)        s += fym * ((code & 8) ? b : a);
-    if (z + 1 < g.nz) s += fzp * ((code & 16) ? b : a);
-    if (z > 0)        s += fzm * ((code & 32) ? b : a);
+    T s = fxp * ((code & 1) ? b : a);
+    s += fxm * ((code & 2) ? b : a);
+    s += fyp * ((code & 4) ? b : a);
+    s += fym * ((code & 8) ? b : a);
+    s += fzp * ((code & 16) ? b : a);
+    s += fzm * ((code & 32) ? b : a);
     s += fc * diag;
     return s;
 }

@@ -10,14 +10,17 @@ namespace ft {
 // the previous inner solve), r64 = b - A x64' in FP64, and the next inner
 // system A e = fp32(r64) set up with e = 0 and zeroed Krylov vectors.
 // Dots (FP64): |r64|^2, |b|^2, |fp32(r64)|^2, fp32(r64).z.
+// Streams: x64, e, code.
 // ===========================================================================
 template <bool BICG>
 struct OpRefine {
     using T = double;
-    using SL = Streams<8, 4, 1>;  // x64, e, code
+    using SL = Streams<8, 4, 1>;
     static constexpr int NV = 4;
     using Shared = Coef<float>;
+    struct Vals { double x; float e; uint32_t code; };
     struct Own { uint32_t code; };
+    struct Out { double x; float r; };
     const CUtensorMap *tmap[SL::N];
     double *x64n;
     float *r, *r0, *p0, *v0;
@@ -25,6 +28,17 @@ struct OpRefine {
 
     __device__ static bool active(const Scalars &sc) { return sc.outer_state == RUNNING; }
     __device__ static void load_shared(Shared &S, const Job &J, int tid) { load_coef<float>(S, J, tid); }
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<double, SL, 0>(st, p, a.x, b.x);
+        sv2<float, SL, 1>(st, p, a.e, b.e);
+        load_code2<SL, 2>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a)
+    {
+        a.x = sv<double, SL, 0>(st, p);
+        a.e = sv<float, SL, 1>(st, p);
+    }
     __device__ void init(const Job &J, Shared &)
     {
         const int cur = J.sc->x64_cur;
@@ -37,40 +51,39 @@ struct OpRefine {
         p0 = (float *)J.p[0];
         v0 = (float *)J.v[0];
     }
-    template <bool INT>
-    __device__ double field(const Geo &, const Coef<double> &, Shared &, const unsigned char *st, const Pt &pt, int,
-                            int, int) const
+    __device__ double field(const Geo &, const Coef<double> &, Shared &, const Vals &v, int, int, int) const
     {
-        return sv<double, SL, 0>(st, pt) + (double)sv<float, SL, 1>(st, pt);
+        return v.x + (double)v.e;
     }
-    template <bool INT>
-    __device__ Own own(const Geo &, const Coef<double> &, Shared &, const unsigned char *st, const Pt &pt, int, int,
-                       int, double &f) const
+    __device__ Own own(const Geo &, const Coef<double> &, Shared &, const Vals &v, int, int, int, double &f) const
     {
-        f = sv<double, SL, 0>(st, pt) + (double)sv<float, SL, 1>(st, pt);
-        return Own{(uint32_t)sv<uint8_t, SL, 2>(st, pt)};
+        f = v.x + (double)v.e;
+        return Own{v.code};
     }
-    template <bool INT>
-    __device__ void apply(const Geo &g, const Coef<double> &C, Shared &S, const Own &o, int64_t i, int x_, int y_,
-                          int z_, double fc, double fxp, double fxm, double fyp, double fym, double fzp, double fzm)
+    __device__ Out apply(const Geo &g, const Coef<double> &C, Shared &S, const Own &o, int x_, int y_, int z_,
+                         double fc, double fxp, double fxm, double fyp, double fym, double fzp, double fzm)
     {
-        const double d = diag_x<double, INT>(C, g, o.code, x_, y_, z_);
-        const double ax = stencil_x<double, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const double d = diag_of<double>(C, g, o.code, x_, y_, z_);
+        const double ax = stencil7<double>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         const double b = rhs_at<double>(C, g, o.code, x_, y_, z_);
         const double res = b - ax;
-        x64n[i] = fc;
         const float r32 = (float)res;
-        r[i] = r32;
-        p0[i] = 0.f;
-        if (BICG) {
-            r0[i] = r32;
-            v0[i] = 0.f;
-        }
-        const float inv = inv_x<float, INT>(S, g, o.code, x_, y_, z_);
+        const float inv = inv_of<float>(S, g, o.code, x_, y_, z_);
         a_r64.add_prod(res, res);
         a_bb.add_prod(b, b);
         a_r32.add_prod((double)r32, (double)r32);
         a_rz.add_prod((double)r32, (double)(r32 * inv));
+        return Out{fc, r32};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0_, bool v1_)
+    {
+        store2<double>(x64n, i, a.x, b.x, v0_, v1_);
+        store2<float>(r, i, a.r, b.r, v0_, v1_);
+        store2<float>(p0, i, 0.f, 0.f, v0_, v1_);
+        if (BICG) {
+            store2<float>(r0, i, a.r, b.r, v0_, v1_);
+            store2<float>(v0, i, 0.f, 0.f, v0_, v1_);
+        }
     }
     __device__ void partials(double (&v)[NV]) const
     {
@@ -139,12 +152,12 @@ struct OpRefine {
 };
 
 // ===========================================================================
-// Pointwise kernels on the same tiling: stencil codes + pore count, the
-// MIXED x64 = x0 initialisation, and the tau flux sum.
+// Pointwise kernels on the same tiling (two x columns per thread): stencil
+// codes + pore count, the MIXED x64 = x0 initialisation, and the tau flux.
 // ===========================================================================
 struct TileCoords {
     int x0, y0, z0, z1, gx, gy;
-    bool vxy;
+    bool v[2];
     int64_t local;
 };
 
@@ -159,15 +172,17 @@ __device__ __forceinline__ TileCoords tile_coords(const Job &J, int tid)
     t.y0 = ty_t * TY;
     t.z0 = tz_t * J.zc;
     t.z1 = min(t.z0 + J.zc, J.nz);
-    t.gx = t.x0 + tid % TX;
-    t.gy = t.y0 + tid / TX;
-    t.vxy = t.gx < J.nx && t.gy < J.ny;
+    t.gx = t.x0 + 2 * (tid % TPR);
+    t.gy = t.y0 + tid / TPR;
+    t.v[0] = t.gx < J.nx && t.gy < J.ny;
+    t.v[1] = t.gx + 1 < J.nx && t.gy < J.ny;
     return t;
 }
 
 // Stencil code of every voxel (bit d: neighbour d solid, clamped at the domain
-// faces; bit 6: self solid) and the number of pore (zero) voxels, as
-// Volume::sumZeroElems counts them (fastlib/src/volume/Volume.cpp:261-272).
+// faces; bit 6: self solid; bit 7: on a domain face) and the number of pore
+// (zero) voxels, as Volume::sumZeroElems counts them
+// (fastlib/src/volume/Volume.cpp:261-272).
 __global__ void __launch_bounds__(NTHREADS) code_kernel(Launch L)
 {
     __shared__ int s_job, s_flag;
@@ -177,25 +192,28 @@ __global__ void __launch_bounds__(NTHREADS) code_kernel(Launch L)
     __syncthreads();
     const Job &J = L.jobs[s_job];
     const TileCoords t = tile_coords(J, tid);
-    const Geo g{J.nx, J.ny, J.nz, 0, 1, J.nx};  // the input mask is unpadded
+    const int nx = J.nx, ny = J.ny, nz = J.nz;
     uint8_t *code = const_cast<uint8_t *>(J.code);
-    const uint8_t *m = J.mask;
+    const uint8_t *m = J.mask;  // unpadded
+    const int64_t sy = nx, sz = (int64_t)nx * ny;
     uint32_t pores = 0;
-    if (t.vxy) {
-        const int x = t.gx, y = t.gy;
+    for (int k = 0; k < 2; k++) {
+        if (!t.v[k]) continue;
+        const int x = t.gx + k, y = t.gy;
         for (int z = t.z0; z < t.z1; ++z) {
-            const int64_t i = g.idx(x, y, z);
-            const int64_t ic = (int64_t)x + (int64_t)J.pitch * ((int64_t)y + (int64_t)g.ny * z);
+            const int64_t i = (int64_t)x + sy * y + sz * z;
+            const int64_t ic = (int64_t)x + (int64_t)J.pitch * ((int64_t)y + (int64_t)ny * z);
             const uint32_t self = __ldg(m + i) != 0;
             pores += self ? 0u : 1u;
             uint32_t c = self << SELF_BIT;
-            c |= (x + 1 < g.nx ? (__ldg(m + i + 1) != 0) : self) << 0;
+            c |= (x + 1 < nx ? (__ldg(m + i + 1) != 0) : self) << 0;
             c |= (x > 0 ? (__ldg(m + i - 1) != 0) : self) << 1;
-            c |= (y + 1 < g.ny ? (__ldg(m + i + g.nx) != 0) : self) << 2;
-            c |= (y > 0 ? (__ldg(m + i - g.nx) != 0) : self) << 3;
-            const int64_t sz = (int64_t)g.nx * g.ny;
-            c |= (z + 1 < g.nz ? (__ldg(m + i + sz) != 0) : self) << 4;
+            c |= (y + 1 < ny ? (__ldg(m + i + sy) != 0) : self) << 2;
+            c |= (y > 0 ? (__ldg(m + i - sy) != 0) : self) << 3;
+            c |= (z + 1 < nz ? (__ldg(m + i + sz) != 0) : self) << 4;
             c |= (z > 0 ? (__ldg(m + i - sz) != 0) : self) << 5;
+            const bool bnd = x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1;
+            c |= (bnd ? 1u : 0u) << BND_BIT;
             code[ic] = (uint8_t)c;
         }
     }
@@ -221,13 +239,15 @@ __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
     const Job &J = L.jobs[s_job];
     const TileCoords t = tile_coords(J, tid);
     const Geo g{J.nx, J.ny, J.nz, J.dir >> 1, (J.dir & 1) ? -1 : 1, J.pitch};
-    if (!t.vxy) return;
     double *x64 = J.x64[0];
     float *e = (float *)J.x;
-    for (int z = t.z0; z < t.z1; ++z) {
-        const int64_t i = g.idx(t.gx, t.gy, z);
-        x64[i] = x0_at<double>(g, t.gx, t.gy, z);
-        e[i] = 0.f;
+    for (int k = 0; k < 2; k++) {
+        if (!t.v[k]) continue;
+        for (int z = t.z0; z < t.z1; ++z) {
+            const int64_t i = g.idx(t.gx + k, t.gy, z);
+            x64[i] = x0_at<double>(g, t.gx + k, t.gy, z);
+            e[i] = 0.f;
+        }
     }
 }
 
@@ -252,11 +272,12 @@ __global__ void __launch_bounds__(NTHREADS) tau_kernel(Launch L, int use_x64)
     const int64_t sstep = g.sgn > 0 ? step : -step;
     const int ext = g.extent();
     Acc<double> acc;
-    if (t.vxy) {
+    for (int k = 0; k < 2; k++) {
+        if (!t.v[k]) continue;
+        const int x = t.gx + k;
         for (int z = t.z0; z < t.z1; ++z) {
-            const int64_t i = g.idx(t.gx, t.gy, z);
-            const int kc = g.coord(t.gx, t.gy, z);
-            const int kn = kc + g.sgn;
+            const int64_t i = g.idx(x, t.gy, z);
+            const int kn = g.coord(x, t.gy, z) + g.sgn;
             const double here = (double)__ldg(c + i);
             double prev = 0.0, dx = 0.5;
             if (kn >= 0 && kn < ext) {

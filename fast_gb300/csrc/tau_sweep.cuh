@@ -2,19 +2,21 @@
 // operations (Op) that plug into it.
 //
 // One thread block owns a TX x TY column tile of one right-hand side and
-// marches the planes z0..z1-1 of its slab.  The state vectors an operation
-// reads arrive through TMA: for every plane, thread 0 issues one
-// cp.async.bulk.tensor tile load per vector (the TX x TY tile plus a
-// one-voxel x/y halo, widened in x to the 16-byte TMA alignment) into a ring
-// of NSTAGE shared-memory stages, each completed on its own mbarrier, so
-// NSTAGE-1 planes of every vector are in flight while the block computes.
-// From a stage the block forms the operand field of the plane (p = z + beta
-// p, y = p/diag, ...) for its tile and halo into a shared plane buffer; the z
-// neighbours of a thread's own column stay in registers.  The operator is
-// applied one plane behind the loads.  Dot products accumulate per thread,
-// reduce per block into a partial slot, and the last block of each
-// right-hand side to arrive sums the partials in a fixed order and advances
-// that right-hand side's scalars.
+// marches the planes z0..z1-1 of its slab; each thread owns two neighbouring
+// x columns.  The state vectors an operation reads arrive through TMA: for
+// every plane, thread 0 issues one cp.async.bulk.tensor tile load per vector
+// (the tile plus a one-voxel x/y halo, widened in x to the 16-byte TMA
+// alignment) into a ring of NSTAGE shared-memory stages, each completed on
+// its own mbarrier, so NSTAGE-1 planes of every vector are in flight while
+// the block computes.  From a stage the block forms the operand field of the
+// plane (p = z + beta p, y = p/diag, ...) for its tile and halo into a shared
+// plane buffer (paired vector stores); the z neighbours of a thread's own
+// columns stay in registers.  The operator is applied one plane behind the
+// loads.  Points outside the domain hold exactly 0 in the plane buffers and
+// registers, so the stencil needs no bounds tests.  Dot products accumulate
+// per thread, reduce per block into a partial slot, and the last block of
+// each right-hand side to arrive sums the partials in a fixed order and
+// advances that right-hand side's scalars.
 //
 // Every mbarrier wait is bounded (%globaltimer, 2 s).  A block whose tile
 // loads do not arrive drains its own copies in flight (again bounded), marks
@@ -88,7 +90,8 @@ __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *tm)
 // ---------------------------------------------------------------------------
 // Shared-memory stage layout.  A stream of element size ES is loaded as a box
 // of box_w(ES) x HY elements starting at (x0 - 16/ES, y0 - 1): the box start
-// and width in x are multiples of 16 bytes.
+// and width in x are multiples of 16 bytes, and the element of x = x0 + 2k
+// sits at an even offset, so a thread's two columns load as one vector.
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr int box_off(int es) { return 16 / es; }
 __host__ __device__ constexpr int box_w(int es) { return TX + 2 * box_off(es); }
@@ -118,69 +121,63 @@ struct Streams {
     }
 };
 
-// A point of the stage tile: its element offset within a box of each
-// element size, for tile row `row` (0..HY-1) and x offset xr = x - x0 (-1..TX).
+// A point of the stage tile: tile row (0..HY-1) and x offset xr = x - x0
+// (-1..TX).
 struct Pt {
-    int o1, o4, o8;
+    int row, xr;
 };
-__device__ __forceinline__ Pt make_pt(int row, int xr)
+
+template <typename E, class SL, int S>
+__device__ __forceinline__ const E *sp(const unsigned char *stage, const Pt &p)
 {
-    return Pt{row * box_w(1) + xr + box_off(1), row * box_w(4) + xr + box_off(4), row * box_w(8) + xr + box_off(8)};
+    constexpr int es = (int)sizeof(E);
+    return reinterpret_cast<const E *>(stage + SL::off(S)) + p.row * box_w(es) + p.xr + box_off(es);
 }
 
-// Element of stream S at point p of a stage.
+// Element of stream S at point p.
 template <typename E, class SL, int S>
 __device__ __forceinline__ E sv(const unsigned char *stage, const Pt &p)
 {
-    constexpr int es = (int)sizeof(E);
-    const int o = es == 1 ? p.o1 : (es == 4 ? p.o4 : p.o8);
-    return reinterpret_cast<const E *>(stage + SL::off(S))[o];
+    return *sp<E, SL, S>(stage, p);
 }
 
-// Diagonal, its inverse and the operator on the interior fast path (all six
-// neighbours inside the domain: table lookups, no boundary tests) or the
-// general path.
-template <typename T, bool INT>
-__device__ __forceinline__ T diag_x(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+// The two elements of stream S at p and p + 1 (p.xr even), as one load.
+template <typename E, class SL, int S>
+__device__ __forceinline__ void sv2(const unsigned char *stage, const Pt &p, E &a, E &b)
 {
-    if constexpr (INT) return C.diag_int[code & 127];
-    else return diag_at<T>(C, g, code, x, y, z);
-}
-template <typename T, bool INT>
-__device__ __forceinline__ T inv_x(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
-{
-    if constexpr (INT) return C.inv_int[code & 127];
-    else return inv_diag_at<T>(C, g, code, x, y, z);
-}
-template <typename T, bool INT>
-__device__ __forceinline__ T stencil_x(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z, T fc,
-                                       T fxp, T fxm, T fyp, T fym, T fzp, T fzm, T diag)
-{
-    if constexpr (INT) {
-        const int self = (code >> SELF_BIT) & 1;
-        const T a = C.face[self][0], b = C.face[self][1];
-        T s = fxp * ((code & 1) ? b : a);
-        s += fxm * ((code & 2) ? b : a);
-        s += fyp * ((code & 4) ? b : a);
-        s += fym * ((code & 8) ? b : a);
-        s += fzp * ((code & 16) ? b : a);
-        s += fzm * ((code & 32) ? b : a);
-        s += fc * diag;
-        return s;
+    const E *q = sp<E, SL, S>(stage, p);
+    if constexpr (sizeof(E) == 4) {
+        const float2 v = *reinterpret_cast<const float2 *>(q);
+        a = v.x;
+        b = v.y;
+    } else if constexpr (sizeof(E) == 8) {
+        const double2 v = *reinterpret_cast<const double2 *>(q);
+        a = v.x;
+        b = v.y;
     } else {
-        return apply_stencil<T>(C, g, code, x, y, z, fc, fxp, fxm, fyp, fym, fzp, fzm, diag);
+        const unsigned short v = *reinterpret_cast<const unsigned short *>(q);
+        a = (E)(v & 0xff);
+        b = (E)(v >> 8);
     }
 }
 
-// Halo slot h (0..NHALO-1) of the shared plane -> (hx, hy) in the buffer.
-__device__ __forceinline__ void halo_slot(int h, int &hx, int &hy)
+template <typename T>
+struct alignas(2 * sizeof(T)) Pair {
+    T a, b;
+};
+
+// Stores a lane pair to p[i], p[i+1] (i even): one vector store when both
+// lanes are inside the domain.
+template <typename T>
+__device__ __forceinline__ void store2(T *p, int64_t i, T a, T b, bool v0, bool v1)
 {
-    if (h < HX) { hx = h; hy = 0; }
-    else if (h < 2 * HX) { hx = h - HX; hy = HY - 1; }
-    else if (h < 2 * HX + TY) { hx = 0; hy = 1 + (h - 2 * HX); }
-    else { hx = HX - 1; hy = 1 + (h - 2 * HX - TY); }
+    if (v0 && v1) {
+        *reinterpret_cast<Pair<T> *>(p + i) = Pair<T>{a, b};
+    } else {
+        if (v0) p[i] = a;
+        if (v1) p[i + 1] = b;
+    }
 }
-constexpr int NHALO = 2 * HX + 2 * TY;
 
 // Dynamic shared memory of a sweep: the stage ring plus 128 bytes to align
 // its base to 128 bytes.
@@ -190,18 +187,24 @@ __host__ __device__ constexpr int sweep_dyn_smem()
     return NSTAGE * Op::SL::stage_bytes() + 128;
 }
 
+// Plane buffer: row stride PW elements; x = x0 + k sits at column k + 2, so
+// thread pairs start at even columns; column 1 holds x0 - 1, column TX + 2
+// holds x0 + TX.
+constexpr int PW = TX + 4;
+
 template <class Op, int NSTAGE>
 __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
 {
     using T = typename Op::T;
     using SL = typename Op::SL;
+    using V = typename Op::Vals;
     constexpr int NV = Op::NV;
     constexpr int SB = SL::stage_bytes();
     extern __shared__ __align__(128) unsigned char dsm[];
     __shared__ __align__(8) uint64_t bars[NSTAGE];
     __shared__ int s_job, s_go, s_flag, s_err;
     __shared__ Coef<T> C;
-    __shared__ T fb[3][HY][HX];
+    __shared__ __align__(16) T fb[3][HY][PW];
     __shared__ double s_red[2 * NV * (NTHREADS / 32)];
     __shared__ typename Op::Shared S;
 
@@ -227,12 +230,10 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
     const int z1 = min(z0 + J.zc, g.nz);
     const int pa = max(z0 - 1, 0), pb = min(z1, g.nz - 1);
     const int NP = pb - pa + 1;
-    const int lx = tid % TX, ly = tid / TX;
-    const int gx = x0 + lx, gy = y0 + ly;
-    const bool vxy = gx < g.nx && gy < g.ny;
-    // The tile and its halo ring lie strictly inside the domain in x and y:
-    // planes away from the z faces then take the interior fast path.
-    const bool blk_int = x0 >= 2 && x0 + TX <= g.nx - 2 && y0 >= 2 && y0 + TY <= g.ny - 2;
+    const int lp = tid % TPR, ly = tid / TPR;
+    const int gx = x0 + 2 * lp, gy = y0 + ly;
+    const bool v0 = gx < g.nx && gy < g.ny;
+    const bool v1 = gx + 1 < g.nx && gy < g.ny;
     const int64_t plane = (int64_t)g.P * g.ny;
     const int64_t i_col = (int64_t)gx + (int64_t)g.P * gy;
 
@@ -263,19 +264,33 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
         for (int q = 0; q < n0; ++q) issue(q);
     }
 
-    int hx = 0, hy = 0, hgx = 0, hgy = 0;
-    const bool has_halo = tid < NHALO;
-    if (has_halo) {
-        halo_slot(tid, hx, hy);
-        hgx = x0 - 1 + hx;
-        hgy = y0 - 1 + hy;
+    // Halo roles: threads 0..TPR-1 the row above the tile, TPR..2TPR-1 the
+    // row below (pairs), then TY threads the column left of the tile and TY
+    // the column right of it (single points).  Corners are never read.
+    int hrow = 0, hcol = 0, hgx = 0, hgy = 0, hkind = 0;
+    if (tid < 2 * TPR) {
+        const int t = tid % TPR;
+        hkind = 1;
+        hrow = tid < TPR ? 0 : HY - 1;
+        hgx = x0 + 2 * t;
+        hgy = tid < TPR ? y0 - 1 : y0 + TY;
+        hcol = 2 * t + 2;
+    } else if (tid < 2 * TPR + 2 * TY) {
+        const int t = tid - 2 * TPR;
+        hkind = 2;
+        hrow = 1 + (t % TY);
+        hgy = y0 + (t % TY);
+        hgx = t < TY ? x0 - 1 : x0 + TX;
+        hcol = t < TY ? 1 : TX + 2;
     }
-    const Pt p_own = make_pt(ly + 1, lx);
-    const Pt p_halo = make_pt(hy, hx - 1);
-    const bool halo_in = has_halo && (unsigned)hgx < (unsigned)g.nx && (unsigned)hgy < (unsigned)g.ny;
+    const bool hin_y = (unsigned)hgy < (unsigned)g.ny;
+    const bool h0 = hin_y && (unsigned)hgx < (unsigned)g.nx;
+    const bool h1 = hin_y && (unsigned)(hgx + 1) < (unsigned)g.nx;
+    const Pt p_own{ly + 1, 2 * lp};
+    const Pt p_halo{hrow, hgx - x0};
 
-    T f_m = T(0), f_c = T(0), f_p = T(0);
-    typename Op::Own o_c{}, o_p{};
+    T fm0 = T(0), fm1 = T(0), fc0 = T(0), fc1 = T(0), fp0 = T(0), fp1 = T(0);
+    typename Op::Own oc0{}, oc1{}, op0{}, op1{};
     int q = 0;
     for (; q < NP; ++q) {
         const int zq = pa + q;
@@ -283,29 +298,30 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
         if (!mbar_wait_bounded(smem_u32(&bars[st]), (uint32_t)((q / NSTAGE) & 1))) s_err = 1;
         const unsigned char *stage = sbase + st * SB;
         const bool out_plane = zq >= z0 && zq < z1;
-        const bool fint = blk_int && zq >= 1 && zq <= g.nz - 2;
-        if (fint) {
-            if (out_plane) o_p = op.template own<true>(g, C, S, stage, p_own, gx, gy, zq, f_p);
-            else f_p = op.template field<true>(g, C, S, stage, p_own, gx, gy, zq);
+        {
+            V a, b;
+            Op::load2(stage, p_own, a, b);
+            fp0 = T(0);
+            fp1 = T(0);
             if (out_plane) {
-                fb[zq % 3][ly + 1][lx + 1] = f_p;
-                if (has_halo) fb[zq % 3][hy][hx] = op.template field<true>(g, C, S, stage, p_halo, hgx, hgy, zq);
-            }
-        } else {
-            if (vxy) {
-                if (out_plane) o_p = op.template own<false>(g, C, S, stage, p_own, gx, gy, zq, f_p);
-                else f_p = op.template field<false>(g, C, S, stage, p_own, gx, gy, zq);
+                if (v0) op0 = op.own(g, C, S, a, gx, gy, zq, fp0);
+                if (v1) op1 = op.own(g, C, S, b, gx + 1, gy, zq, fp1);
+                *reinterpret_cast<Pair<T> *>(&fb[zq % 3][ly + 1][2 * lp + 2]) = Pair<T>{fp0, fp1};
             } else {
-                f_p = T(0);
+                if (v0) fp0 = op.field(g, C, S, a, gx, gy, zq);
+                if (v1) fp1 = op.field(g, C, S, b, gx + 1, gy, zq);
             }
-            if (out_plane) {
-                fb[zq % 3][ly + 1][lx + 1] = f_p;
-                if (has_halo) {
-                    T v = T(0);
-                    if (halo_in) v = op.template field<false>(g, C, S, stage, p_halo, hgx, hgy, zq);
-                    fb[zq % 3][hy][hx] = v;
-                }
-            }
+        }
+        if (out_plane && hkind == 1) {
+            V a, b;
+            Op::load2(stage, p_halo, a, b);
+            const T f0 = h0 ? op.field(g, C, S, a, hgx, hgy, zq) : T(0);
+            const T f1 = h1 ? op.field(g, C, S, b, hgx + 1, hgy, zq) : T(0);
+            *reinterpret_cast<Pair<T> *>(&fb[zq % 3][hrow][hcol]) = Pair<T>{f0, f1};
+        } else if (out_plane && hkind == 2) {
+            V a;
+            Op::load1(stage, p_halo, a);
+            fb[zq % 3][hrow][hcol] = h0 ? op.field(g, C, S, a, hgx, hgy, zq) : T(0);
         }
         __syncthreads();
         if (s_err) break;
@@ -315,19 +331,24 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
             issue(q + NSTAGE);
         }
         const int zs = zq - 1;
-        if (zs >= z0 && zs < z1 && vxy) {
-            const T(*P)[HX] = fb[zs % 3];
+        if (zs >= z0 && zs < z1 && (v0 || v1)) {
+            const T(*P)[PW] = fb[zs % 3];
+            const Pair<T> left = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp]);
+            const Pair<T> right = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp + 4]);
+            const Pair<T> up = *reinterpret_cast<const Pair<T> *>(&P[ly + 2][2 * lp + 2]);
+            const Pair<T> dn = *reinterpret_cast<const Pair<T> *>(&P[ly][2 * lp + 2]);
             const int64_t i = i_col + plane * zs;
-            if (blk_int && zs >= 1 && zs <= g.nz - 2)
-                op.template apply<true>(g, C, S, o_c, i, gx, gy, zs, f_c, P[ly + 1][lx + 2], P[ly + 1][lx],
-                                        P[ly + 2][lx + 1], P[ly][lx + 1], f_p, f_m);
-            else
-                op.template apply<false>(g, C, S, o_c, i, gx, gy, zs, f_c, P[ly + 1][lx + 2], P[ly + 1][lx],
-                                         P[ly + 2][lx + 1], P[ly][lx + 1], f_p, f_m);
+            typename Op::Out r0{}, r1{};
+            if (v0) r0 = op.apply(g, C, S, oc0, gx, gy, zs, fc0, fc1, left.b, up.a, dn.a, fp0, fm0);
+            if (v1) r1 = op.apply(g, C, S, oc1, gx + 1, gy, zs, fc1, right.a, fc0, up.b, dn.b, fp1, fm1);
+            op.store(i, r0, r1, v0, v1);
         }
-        f_m = f_c;
-        f_c = f_p;
-        o_c = o_p;
+        fm0 = fc0;
+        fm1 = fc1;
+        fc0 = fp0;
+        fc1 = fp1;
+        oc0 = op0;
+        oc1 = op1;
     }
 
     if (s_err) {
@@ -343,11 +364,17 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
         return;
     }
     // The last plane of the volume has no z+1 neighbour: apply it here.
-    if (pb == z1 - 1 && vxy) {
+    if (pb == z1 - 1 && (v0 || v1)) {
         const int zs = z1 - 1;
-        const T(*P)[HX] = fb[zs % 3];
-        op.template apply<false>(g, C, S, o_c, i_col + plane * zs, gx, gy, zs, f_c, P[ly + 1][lx + 2],
-                                 P[ly + 1][lx], P[ly + 2][lx + 1], P[ly][lx + 1], T(0), f_m);
+        const T(*P)[PW] = fb[zs % 3];
+        const Pair<T> left = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp]);
+        const Pair<T> right = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp + 4]);
+        const Pair<T> up = *reinterpret_cast<const Pair<T> *>(&P[ly + 2][2 * lp + 2]);
+        const Pair<T> dn = *reinterpret_cast<const Pair<T> *>(&P[ly][2 * lp + 2]);
+        typename Op::Out r0{}, r1{};
+        if (v0) r0 = op.apply(g, C, S, oc0, gx, gy, zs, fc0, fc1, left.b, up.a, dn.a, T(0), fm0);
+        if (v1) r1 = op.apply(g, C, S, oc1, gx + 1, gy, zs, fc1, right.a, fc0, up.b, dn.b, T(0), fm1);
+        op.store(i_col + plane * zs, r0, r1, v0, v1);
     }
 
     T v[NV];
@@ -365,9 +392,24 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
 }
 
 // ---------------------------------------------------------------------------
-// Helpers shared by the ops.
+// Operation interface.  An op names its streams (SL, code last), loads one
+// point's stream values (Vals) for a lane pair (load2) or a single point
+// (load1), forms the operand field at a point (field), the same plus what the
+// point's own update needs (own -> Own), applies the update from the
+// stencil of the field (apply -> Out, accumulating its dot products), and
+// writes a lane pair's outputs (store).
 // ---------------------------------------------------------------------------
 struct NoShared {};
+struct NoOut {};
+
+template <class SL, int S>
+__device__ __forceinline__ void load_code2(const unsigned char *st, const Pt &p, uint32_t &a, uint32_t &b)
+{
+    uint8_t ca, cb;
+    sv2<uint8_t, SL, S>(st, p, ca, cb);
+    a = ca;
+    b = cb;
+}
 
 // ===========================================================================
 // Setup of a pure-precision solve (F64 or F32): x = x0, r = b - A x0, and the
@@ -381,49 +423,56 @@ struct OpInit {
     using SL = Streams<1>;
     static constexpr int NV = 3;
     using Shared = NoShared;
+    struct Vals { uint32_t code; };
     struct Own { uint32_t code; };
+    struct Out { T x, r; };
     const CUtensorMap *tmap[SL::N];
     T *x, *r, *r0, *p0, *v0;
     Acc<T> bb, rr, rz;
 
     __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
     __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        load_code2<SL, 0>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a) { a.code = sv<uint8_t, SL, 0>(st, p); }
     __device__ void init(const Job &J, Shared &)
     {
         tmap[0] = &J.tm[TM_CODE];
         x = (T *)J.x; r = (T *)J.r[0]; r0 = (T *)J.r0; p0 = (T *)J.p[0]; v0 = (T *)J.v[0];
     }
-    template <bool INT>
-    __device__ T field(const Geo &g, const Coef<T> &, Shared &, const unsigned char *, const Pt &, int x_, int y_,
-                       int z_) const
+    __device__ T field(const Geo &g, const Coef<T> &, Shared &, const Vals &, int x_, int y_, int z_) const
     {
         return x0_at<T>(g, x_, y_, z_);
     }
-    template <bool INT>
-    __device__ Own own(const Geo &g, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    __device__ Own own(const Geo &g, const Coef<T> &, Shared &, const Vals &v, int x_, int y_, int z_, T &f) const
     {
         f = x0_at<T>(g, x_, y_, z_);
-        return Own{(uint32_t)sv<uint8_t, SL, 0>(st, pt)};
+        return Own{v.code};
     }
-    template <bool INT>
-    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
-                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+                         T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
-        const T ax = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
+        const T ax = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         const T b = rhs_at<T>(C, g, o.code, x_, y_, z_);
         const T res = b - ax;
-        x[i] = fc;
-        r[i] = res;
-        p0[i] = T(0);
-        if (BICG) {
-            r0[i] = res;
-            v0[i] = T(0);
-        }
-        const T inv = INT ? C.inv_int[o.code & 127] : (g.interior(x_, y_, z_) ? C.inv_int[o.code & 127] : T(1) / d);
+        const T inv = (o.code & (1u << BND_BIT)) ? T(1) / d : C.inv_int[o.code & 127];
         bb.add_prod(b, b);
         rr.add_prod(res, res);
         rz.add_prod(res, res * inv);
+        return Out{fc, res};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0_, bool v1_)
+    {
+        store2<T>(x, i, a.x, b.x, v0_, v1_);
+        store2<T>(r, i, a.r, b.r, v0_, v1_);
+        store2<T>(p0, i, T(0), T(0), v0_, v1_);
+        if (BICG) {
+            store2<T>(r0, i, a.r, b.r, v0_, v1_);
+            store2<T>(v0, i, T(0), T(0), v0_, v1_);
+        }
     }
     __device__ void partials(T (&v)[NV]) const { v[0] = bb.hi(); v[1] = rr.hi(); v[2] = rz.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
@@ -472,7 +521,9 @@ struct OpCG1 {
     using SL = Streams<sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 1;
     using Shared = NoShared;
+    struct Vals { T r, p; uint32_t code; };
     struct Own { uint32_t code; };
+    struct Out { T p; };
     const CUtensorMap *tmap[SL::N];
     T *pnew;
     T beta;
@@ -480,6 +531,18 @@ struct OpCG1 {
 
     __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
     __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<T, SL, 0>(st, p, a.r, b.r);
+        sv2<T, SL, 1>(st, p, a.p, b.p);
+        load_code2<SL, 2>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a)
+    {
+        a.r = sv<T, SL, 0>(st, p);
+        a.p = sv<T, SL, 1>(st, p);
+        a.code = sv<uint8_t, SL, 2>(st, p);
+    }
     __device__ void init(const Job &J, Shared &)
     {
         const int par = (int)(J.sc->iter & 1);
@@ -489,33 +552,27 @@ struct OpCG1 {
         pnew = (T *)J.p[par ^ 1];
         beta = (T)J.sc->beta;
     }
-    template <bool INT>
-    __device__ __forceinline__ T pval(const Geo &g, const Coef<T> &C, const unsigned char *st, const Pt &pt,
-                                      int x_, int y_, int z_, uint32_t c) const
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_) const
     {
-        const T zi = sv<T, SL, 0>(st, pt) * inv_x<T, INT>(C, g, c, x_, y_, z_);
-        return sv<T, SL, 1>(st, pt) * beta + zi;  // __aAddAlphaBKernel: p = p*beta + z
+        const T zi = v.r * inv_of<T>(C, g, v.code, x_, y_, z_);
+        return v.p * beta + zi;  // __aAddAlphaBKernel: p = p*beta + z
     }
-    template <bool INT>
-    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &S, const Vals &v, int x_, int y_, int z_, T &f) const
     {
-        return pval<INT>(g, C, st, pt, x_, y_, z_, sv<uint8_t, SL, 2>(st, pt));
+        f = field(g, C, S, v, x_, y_, z_);
+        return Own{v.code};
     }
-    template <bool INT>
-    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+                         T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const uint32_t c = sv<uint8_t, SL, 2>(st, pt);
-        f = pval<INT>(g, C, st, pt, x_, y_, z_, c);
-        return Own{c};
-    }
-    template <bool INT>
-    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
-                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
-    {
-        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
-        const T q = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
-        pnew[i] = fc;
+        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
+        const T q = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         pap.add_prod(fc, q);
+        return Out{fc};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0, bool v1)
+    {
+        store2<T>(pnew, i, a.p, b.p, v0, v1);
     }
     __device__ void partials(T (&v)[NV]) const { v[0] = pap.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
@@ -535,7 +592,9 @@ struct OpCG2 {
     using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 2;
     using Shared = NoShared;
+    struct Vals { T p, x, r; uint32_t code; };
     struct Own { uint32_t code; T x, r; };
+    struct Out { T x, r; };
     const CUtensorMap *tmap[SL::N];
     T *x, *r;
     T alpha;
@@ -543,6 +602,14 @@ struct OpCG2 {
 
     __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
     __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<T, SL, 0>(st, p, a.p, b.p);
+        sv2<T, SL, 1>(st, p, a.x, b.x);
+        sv2<T, SL, 2>(st, p, a.r, b.r);
+        load_code2<SL, 3>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a) { a.p = sv<T, SL, 0>(st, p); }
     __device__ void init(const Job &J, Shared &)
     {
         const int par = (int)(J.sc->iter & 1);
@@ -554,30 +621,28 @@ struct OpCG2 {
         r = (T *)J.r[0];
         alpha = (T)J.sc->alpha;
     }
-    template <bool INT>
-    __device__ T field(const Geo &, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    __device__ T field(const Geo &, const Coef<T> &, Shared &, const Vals &v, int, int, int) const { return v.p; }
+    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const Vals &v, int, int, int, T &f) const
     {
-        return sv<T, SL, 0>(st, pt);
+        f = v.p;
+        return Own{v.code, v.x, v.r};
     }
-    template <bool INT>
-    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+                         T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        f = sv<T, SL, 0>(st, pt);
-        return Own{(uint32_t)sv<uint8_t, SL, 3>(st, pt), sv<T, SL, 1>(st, pt), sv<T, SL, 2>(st, pt)};
-    }
-    template <bool INT>
-    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
-                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
-    {
-        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
-        const T q = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
+        const T q = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         const T xn = o.x + alpha * fc;        // __aAddBetaBKernel(x, p, alpha)
         const T rn = o.r + (-alpha) * q;      // __aAddBetaBKernel(r, ap, -alpha)
-        x[i] = xn;
-        r[i] = rn;
-        const T inv = INT ? C.inv_int[o.code & 127] : (g.interior(x_, y_, z_) ? C.inv_int[o.code & 127] : T(1) / d);
+        const T inv = (o.code & (1u << BND_BIT)) ? T(1) / d : C.inv_int[o.code & 127];
         rr.add_prod(rn, rn);
         rz.add_prod(rn, rn * inv);
+        return Out{xn, rn};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0, bool v1)
+    {
+        store2<T>(x, i, a.x, b.x, v0, v1);
+        store2<T>(r, i, a.r, b.r, v0, v1);
     }
     __device__ void partials(T (&v)[NV]) const { v[0] = rr.hi(); v[1] = rz.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
@@ -615,13 +680,21 @@ struct OpBiRestart {
     using SL = Streams<sizeof(TT), 1>;
     static constexpr int NV = 1;
     using Shared = NoShared;
+    struct Vals { T x; uint32_t code; };
     struct Own { uint32_t code; };
+    struct Out { T r; };
     const CUtensorMap *tmap[SL::N];
     T *r, *r0;
     Acc<T> rr;
 
     __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING && sc.restart != 0; }
     __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<T, SL, 0>(st, p, a.x, b.x);
+        load_code2<SL, 1>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a) { a.x = sv<T, SL, 0>(st, p); }
     __device__ void init(const Job &J, Shared &)
     {
         const int par = (int)(J.sc->iter & 1);
@@ -630,27 +703,25 @@ struct OpBiRestart {
         r = (T *)J.r[par];
         r0 = (T *)J.r0;
     }
-    template <bool INT>
-    __device__ T field(const Geo &, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    __device__ T field(const Geo &, const Coef<T> &, Shared &, const Vals &v, int, int, int) const { return v.x; }
+    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const Vals &v, int, int, int, T &f) const
     {
-        return sv<T, SL, 0>(st, pt);
+        f = v.x;
+        return Own{v.code};
     }
-    template <bool INT>
-    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+                         T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        f = sv<T, SL, 0>(st, pt);
-        return Own{(uint32_t)sv<uint8_t, SL, 1>(st, pt)};
-    }
-    template <bool INT>
-    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
-                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
-    {
-        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
-        const T ax = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
+        const T ax = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         const T res = rhs_at<T>(C, g, o.code, x_, y_, z_) - ax;
-        r[i] = res;
-        r0[i] = res;
         rr.add_prod(res, res);
+        return Out{res};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0, bool v1)
+    {
+        store2<T>(r, i, a.r, b.r, v0, v1);
+        store2<T>(r0, i, a.r, b.r, v0, v1);
     }
     __device__ void partials(T (&v)[NV]) const { v[0] = rr.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
@@ -675,7 +746,9 @@ struct OpBi1 {
     using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 1;
     using Shared = NoShared;
+    struct Vals { T r, p, v, r0; uint32_t code; };
     struct Own { uint32_t code; T p, r0; };
+    struct Out { T p, v; };
     const CUtensorMap *tmap[SL::N];
     T *pnew, *vnew;
     T beta, nw;
@@ -683,6 +756,21 @@ struct OpBi1 {
 
     __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
     __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<T, SL, 0>(st, p, a.r, b.r);
+        sv2<T, SL, 1>(st, p, a.p, b.p);
+        sv2<T, SL, 2>(st, p, a.v, b.v);
+        sv2<T, SL, 3>(st, p, a.r0, b.r0);
+        load_code2<SL, 4>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a)
+    {
+        a.r = sv<T, SL, 0>(st, p);
+        a.p = sv<T, SL, 1>(st, p);
+        a.v = sv<T, SL, 2>(st, p);
+        a.code = sv<uint8_t, SL, 4>(st, p);
+    }
     __device__ void init(const Job &J, Shared &)
     {
         const int par = (int)(J.sc->iter & 1);
@@ -696,33 +784,30 @@ struct OpBi1 {
         beta = (T)J.sc->beta;
         nw = (T)(-J.sc->omega);
     }
-    __device__ __forceinline__ T pval(const unsigned char *st, const Pt &pt) const
+    // __aPlusBetaBGammaPlusCKernel: p = beta*(p + (-w)*v) + r
+    __device__ __forceinline__ T pval(const Vals &v) const { return beta * (v.p + nw * v.v) + v.r; }
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_) const
     {
-        // __aPlusBetaBGammaPlusCKernel: p = beta*(p + (-w)*v) + r
-        return beta * (sv<T, SL, 1>(st, pt) + nw * sv<T, SL, 2>(st, pt)) + sv<T, SL, 0>(st, pt);
+        return pval(v) * inv_of<T>(C, g, v.code, x_, y_, z_);
     }
-    template <bool INT>
-    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_, T &f) const
     {
-        return pval(st, pt) * inv_x<T, INT>(C, g, sv<uint8_t, SL, 4>(st, pt), x_, y_, z_);
+        const T pn = pval(v);
+        f = pn * inv_of<T>(C, g, v.code, x_, y_, z_);
+        return Own{v.code, pn, v.r0};
     }
-    template <bool INT>
-    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+                         T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const uint32_t c = sv<uint8_t, SL, 4>(st, pt);
-        const T pn = pval(st, pt);
-        f = pn * inv_x<T, INT>(C, g, c, x_, y_, z_);
-        return Own{c, pn, sv<T, SL, 3>(st, pt)};
-    }
-    template <bool INT>
-    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
-                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
-    {
-        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
-        const T vn = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
-        pnew[i] = o.p;
-        vnew[i] = vn;
+        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
+        const T vn = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         r0v.add_prod(o.r0, vn);
+        return Out{o.p, vn};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0, bool v1)
+    {
+        store2<T>(pnew, i, a.p, b.p, v0, v1);
+        store2<T>(vnew, i, a.v, b.v, v0, v1);
     }
     __device__ void partials(T (&v)[NV]) const { v[0] = r0v.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
@@ -741,13 +826,27 @@ struct OpBi2 {
     using SL = Streams<sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 2;
     using Shared = NoShared;
+    struct Vals { T r, v; uint32_t code; };
     struct Own { uint32_t code; T s; };
+    using Out = NoOut;
     const CUtensorMap *tmap[SL::N];
     T nalpha;
     Acc<T> ts, tt;
 
     __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
     __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<T, SL, 0>(st, p, a.r, b.r);
+        sv2<T, SL, 1>(st, p, a.v, b.v);
+        load_code2<SL, 2>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a)
+    {
+        a.r = sv<T, SL, 0>(st, p);
+        a.v = sv<T, SL, 1>(st, p);
+        a.code = sv<uint8_t, SL, 2>(st, p);
+    }
     __device__ void init(const Job &J, Shared &)
     {
         const int par = (int)(J.sc->iter & 1);
@@ -756,32 +855,27 @@ struct OpBi2 {
         tmap[2] = &J.tm[TM_CODE];
         nalpha = (T)(-J.sc->alpha);
     }
-    __device__ __forceinline__ T sval(const unsigned char *st, const Pt &pt) const
+    __device__ __forceinline__ T sval(const Vals &v) const { return v.r + nalpha * v.v; }  // s = r + (-alpha) v
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_) const
     {
-        return sv<T, SL, 0>(st, pt) + nalpha * sv<T, SL, 1>(st, pt);  // s = r + (-alpha) v
+        return sval(v) * inv_of<T>(C, g, v.code, x_, y_, z_);
     }
-    template <bool INT>
-    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_, T &f) const
     {
-        return sval(st, pt) * inv_x<T, INT>(C, g, sv<uint8_t, SL, 2>(st, pt), x_, y_, z_);
+        const T s = sval(v);
+        f = s * inv_of<T>(C, g, v.code, x_, y_, z_);
+        return Own{v.code, s};
     }
-    template <bool INT>
-    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+                         T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const uint32_t c = sv<uint8_t, SL, 2>(st, pt);
-        const T s = sval(st, pt);
-        f = s * inv_x<T, INT>(C, g, c, x_, y_, z_);
-        return Own{c, s};
-    }
-    template <bool INT>
-    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t, int x_, int y_, int z_, T fc,
-                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
-    {
-        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
-        const T t = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
+        const T t = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         ts.add_prod(t, o.s);
         tt.add_prod(t, t);
+        return Out{};
     }
+    __device__ void store(int64_t, const Out &, const Out &, bool, bool) {}
     __device__ void partials(T (&v_)[NV]) const { v_[0] = ts.hi(); v_[1] = tt.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
     {
@@ -802,7 +896,9 @@ struct OpBi3 {
     using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 2;
     using Shared = NoShared;
+    struct Vals { T r, v, p, x, r0; uint32_t code; };
     struct Own { uint32_t code; T s, x, y, r0; };
+    struct Out { T x, r; };
     const CUtensorMap *tmap[SL::N];
     T *x, *rnew;
     T alpha, omega, nalpha, nomega;
@@ -810,6 +906,21 @@ struct OpBi3 {
 
     __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
     __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<T, SL, 0>(st, p, a.r, b.r);
+        sv2<T, SL, 1>(st, p, a.v, b.v);
+        sv2<T, SL, 2>(st, p, a.p, b.p);
+        sv2<T, SL, 3>(st, p, a.x, b.x);
+        sv2<T, SL, 4>(st, p, a.r0, b.r0);
+        load_code2<SL, 5>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a)
+    {
+        a.r = sv<T, SL, 0>(st, p);
+        a.v = sv<T, SL, 1>(st, p);
+        a.code = sv<uint8_t, SL, 5>(st, p);
+    }
     __device__ void init(const Job &J, Shared &)
     {
         const int par = (int)(J.sc->iter & 1);
@@ -826,35 +937,33 @@ struct OpBi3 {
         nalpha = -alpha;
         nomega = -omega;
     }
-    __device__ __forceinline__ T sval(const unsigned char *st, const Pt &pt) const
+    __device__ __forceinline__ T sval(const Vals &v) const { return v.r + nalpha * v.v; }
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_) const
     {
-        return sv<T, SL, 0>(st, pt) + nalpha * sv<T, SL, 1>(st, pt);
+        return sval(v) * inv_of<T>(C, g, v.code, x_, y_, z_);
     }
-    template <bool INT>
-    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_) const
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_, T &f) const
     {
-        return sval(st, pt) * inv_x<T, INT>(C, g, sv<uint8_t, SL, 5>(st, pt), x_, y_, z_);
-    }
-    template <bool INT>
-    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const unsigned char *st, const Pt &pt, int x_, int y_, int z_, T &f) const
-    {
-        const uint32_t c = sv<uint8_t, SL, 5>(st, pt);
-        const T s = sval(st, pt);
-        const T inv = inv_x<T, INT>(C, g, c, x_, y_, z_);
+        const T s = sval(v);
+        const T inv = inv_of<T>(C, g, v.code, x_, y_, z_);
         f = s * inv;
-        return Own{c, s, sv<T, SL, 3>(st, pt), sv<T, SL, 2>(st, pt) * inv, sv<T, SL, 4>(st, pt)};
+        return Own{v.code, s, v.x, v.p * inv, v.r0};
     }
-    template <bool INT>
-    __device__ void apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int64_t i, int x_, int y_, int z_, T fc,
-                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+                         T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_x<T, INT>(C, g, o.code, x_, y_, z_);
-        const T t = stencil_x<T, INT>(C, g, o.code, x_, y_, z_, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
-        x[i] = o.x + (alpha * o.y + omega * fc);   // __ABC_BetaGammaKernel: x += a*y + w*z
-        const T rn = o.s + nomega * t;             // __aPlusBetaBKernel(s, t, r, -w)
-        rnew[i] = rn;
+        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
+        const T t = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T xn = o.x + (alpha * o.y + omega * fc);   // __ABC_BetaGammaKernel: x += a*y + w*z
+        const T rn = o.s + nomega * t;                   // __aPlusBetaBKernel(s, t, r, -w)
         r0r.add_prod(o.r0, rn);
         rr.add_prod(rn, rn);
+        return Out{xn, rn};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0, bool v1)
+    {
+        store2<T>(x, i, a.x, b.x, v0, v1);
+        store2<T>(rnew, i, a.r, b.r, v0, v1);
     }
     __device__ void partials(T (&v_)[NV]) const { v_[0] = r0r.hi(); v_[1] = rr.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])

@@ -6,18 +6,23 @@
 namespace ft {
 
 // Tile of one thread block: TX x TY columns marching over ZC planes in z.
-constexpr int TX = 32;
+// Each thread owns two neighbouring x columns (LANES), so a row of TX
+// voxels is TPR threads.
+constexpr int TX = 64;
 constexpr int TY = 8;
-constexpr int NTHREADS = TX * TY;
-constexpr int HX = TX + 2;   // tile + 1-voxel halo
-constexpr int HY = TY + 2;
+constexpr int LANES = 2;
+constexpr int TPR = TX / LANES;
+constexpr int NTHREADS = TPR * TY;
+constexpr int HY = TY + 2;   // tile rows + one halo row on each side
 constexpr int NPART = 4;     // partial sums per block per kernel
 
 // Stencil code byte: bit d (d = 0..5, Dir order X_POS, X_NEG, Y_POS, Y_NEG,
-// Z_POS, Z_NEG) = neighbour d is solid; bit 6 = the voxel itself is solid.
+// Z_POS, Z_NEG) = neighbour d is solid; bit 6 = the voxel itself is solid;
+// bit 7 = the voxel lies on a face of the domain (some neighbour is outside).
 // Out-of-domain neighbours repeat the voxel's own bit (the reference's
 // clamped neighbour, fastlib/src/solver/Diffusion.cpp:51-62).
 constexpr int SELF_BIT = 6;
+constexpr int BND_BIT = 7;
 
 enum SolveState : int32_t {
     RUNNING = 0,
