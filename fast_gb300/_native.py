@@ -31,7 +31,7 @@ class fast_tau_result(C.Structure):
 
 
 K_COUNT = 16
-KERNEL_NAMES = ["code", "init", "cg1", "cg2", "bi_restart", "bi1", "bi2", "bi3", "refine", "init64", "tau"]
+KERNEL_NAMES = ["code", "init", "cg1", "cg2", "bi_restart", "bi1", "bi2", "bi3", "replace", "init64", "tau"]
 FLAG_PROFILE = 1
 
 
@@ -57,6 +57,12 @@ SIGNATURES = {
     "fast_tau_last_stats": (C.c_int, [C.POINTER(fast_tau_stats)]),
     "fast_porosity_device_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_uint64),
                                                C.POINTER(C.c_double), C.c_void_p]),
+    "fast_ccl_label": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint8, C.c_void_p,
+                                 C.POINTER(C.c_uint32), C.c_void_p, C.c_uint64]),
+    "fast_ccl_label_device": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint8, C.c_void_p,
+                                        C.POINTER(C.c_uint32), C.c_void_p, C.c_uint64, C.c_void_p]),
+    "fast_ccl_boundary_device": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint32, C.c_void_p,
+                                           C.c_void_p]),
     "fast_last_error": (C.c_char_p, []),
     "fast_version": (C.c_char_p, []),
     "fast_gen_spheres": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_double,

@@ -38,6 +38,7 @@ static void dispatch(Step s, const Launch &L, cudaStream_t st)
     case Step::BI1: go<OpBi1<T, ST>>(L, st); break;
     case Step::BI2: go<OpBi2<T, ST>>(L, st); break;
     case Step::BI3: go<OpBi3<T, ST>>(L, st); break;
+    default: break;  // replacement steps are MIXED-only (kern_misc.cu)
     }
 }
 

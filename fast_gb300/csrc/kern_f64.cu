@@ -36,6 +36,7 @@ void launch_pure_f64(Step s, const Launch &L, cudaStream_t st)
     case Step::BI1: go<OpBi1<T, T>>(L, st); break;
     case Step::BI2: go<OpBi2<T, T>>(L, st); break;
     case Step::BI3: go<OpBi3<T, T>>(L, st); break;
+    default: break;  // replacement steps are MIXED-only (kern_misc.cu)
     }
 }
 

@@ -1,4 +1,4 @@
-// Refinement, tau, stencil-code and initialisation kernels.
+// Residual replacement, tau, stencil-code and initialisation kernels.
 #include "tau_launch.h"
 #include "tau_misc.cuh"
 
@@ -6,24 +6,24 @@ namespace ft {
 
 constexpr int kStages = 3;
 
-void launch_refine(bool bicg, const Launch &L, cudaStream_t st)
+void launch_replace(bool bicg, const Launch &L, cudaStream_t st)
 {
     if (bicg)
-        sweep_kernel<OpRefine<true>, kStages>
-            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpRefine<true>, kStages>(), st>>>(L);
+        sweep_kernel<OpReplace<true>, kStages>
+            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpReplace<true>, kStages>(), st>>>(L);
     else
-        sweep_kernel<OpRefine<false>, kStages>
-            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpRefine<false>, kStages>(), st>>>(L);
+        sweep_kernel<OpReplace<false>, kStages>
+            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpReplace<false>, kStages>(), st>>>(L);
 }
 
 cudaError_t configure_misc()
 {
-    cudaError_t a = cudaFuncSetAttribute(sweep_kernel<OpRefine<true>, kStages>,
+    cudaError_t a = cudaFuncSetAttribute(sweep_kernel<OpReplace<true>, kStages>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         sweep_dyn_smem<OpRefine<true>, kStages>());
-    cudaError_t b = cudaFuncSetAttribute(sweep_kernel<OpRefine<false>, kStages>,
+                                         sweep_dyn_smem<OpReplace<true>, kStages>());
+    cudaError_t b = cudaFuncSetAttribute(sweep_kernel<OpReplace<false>, kStages>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         sweep_dyn_smem<OpRefine<false>, kStages>());
+                                         sweep_dyn_smem<OpReplace<false>, kStages>());
     return a != cudaSuccess ? a : b;
 }
 

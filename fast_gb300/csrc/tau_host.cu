@@ -161,6 +161,8 @@ int kind_of(Step s)
     case Step::BI1: return FAST_K_BI1;
     case Step::BI2: return FAST_K_BI2;
     case Step::BI3: return FAST_K_BI3;
+    case Step::REPLACE_CG:
+    case Step::REPLACE_BI: return FAST_K_REPLACE;
     }
     return FAST_K_COUNT - 1;
 }
@@ -303,20 +305,25 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
 {
     cudaStream_t st = E.stream;
     const int chunk = std::max(1, env_int("FAST_TAU_CHUNK", 16));
-    if (env_int("FAST_TAU_TRACE", 0) >= 2) {
-        // Trace: direct launches, scalars of job 0 printed after each kernel.
+    const int trace = env_int("FAST_TAU_TRACE", 0);
+    if (trace >= 2) {
+        // Trace: direct launches, scalars of job 0 printed after each kernel
+        // (level 2) or after each iteration (level 3).
         for (uint64_t it = 0; it < max_iter + 2; it++) {
             bool running = false;
-            for (Step s : steps) {
+            for (size_t k = 0; k < steps.size(); k++) {
+                const Step s = steps[k];
                 launch(s, L, st);
+                if (trace >= 3 && k + 1 < steps.size()) continue;
                 CU(cudaMemcpyAsync(E.h_sc, d_sc, sizeof(Scalars) * njobs, cudaMemcpyDeviceToHost, st));
                 CU(cudaStreamSynchronize(st));
                 const Scalars &S = E.h_sc[0];
                 fprintf(stderr,
                         "trace step %d iter %llu state %d rsq %.6e zr %.6e alpha %.6e beta %.6e rho %.6e omega %.6e "
-                        "dots %.6e %.6e %.6e\n",
+                        "dots %.6e %.6e %.6e r0sq %.6e rsqmax %.6e r64sq %.6e b64sq %.6e repl %d nrepl %d restarts %llu\n",
                         (int)s, (unsigned long long)S.iter, S.state, S.rsq, S.zr, S.alpha, S.beta, S.rho, S.omega,
-                        S.dbg[0], S.dbg[1], S.dbg[2]);
+                        S.dbg[0], S.dbg[1], S.dbg[2], S.r0_sq, S.rsq_max, S.r64_sq, S.b64_sq, S.replace,
+                        S.outer_steps, (unsigned long long)S.restarts);
             }
             for (int j = 0; j < njobs; j++) running |= (E.h_sc[j].state == RUNNING);
             if (!running) break;
@@ -382,14 +389,17 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
 
 void dispatch_f64(Step s, const Launch &L, cudaStream_t st) { launch_pure_f64(s, L, st); }
 void dispatch_f32(Step s, const Launch &L, cudaStream_t st) { launch_pure_f32(s, L, st); }
-void dispatch_mixed(Step s, const Launch &L, cudaStream_t st) { launch_mixed_inner(s, L, st); }
+void dispatch_mixed(Step s, const Launch &L, cudaStream_t st)
+{
+    if (s == Step::REPLACE_CG || s == Step::REPLACE_BI) launch_replace(s == Step::REPLACE_BI, L, st);
+    else launch_mixed_inner(s, L, st);
+}
 
 int status_of(int state)
 {
     switch (state) {
     case CONVERGED: return FAST_OK;
     case DIVERGED: return FAST_DIVERGED;
-    case STALLED: return FAST_NO_CONVERGENCE;
     case FAULT: return FAST_TIMEOUT;
     case RUNNING: return FAST_TIMEOUT;
     default: return FAST_NO_CONVERGENCE;  // MAXITER, ZERO_RHS (CG.cu:41-44 returns false)
@@ -513,11 +523,14 @@ int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64
         S.div_thresh = 10e+10 / h2;  // |r|^2 > 1e11 in the reference's h-scaled units
         S.eps2 = (prec == FAST_PREC_F64) ? (double)DBL_EPSILON * DBL_EPSILON
                                          : (double)FLT_EPSILON * (double)FLT_EPSILON;
-        S.state = mixed ? CONVERGED : RUNNING;
+        S.state = RUNNING;
         S.tol_outer = P.tolerance;
-        S.inner_floor = env_double("FAST_TAU_INNER_TOL", 1e-4);
-        S.max_total = P.max_iter;
-        S.outer_state = RUNNING;
+        // MIXED: the first step is a replacement with restart (x64 = x0, e = 0).
+        S.replace = mixed ? 2 : 0;
+        const double delta = env_double("FAST_TAU_REPLACE_DELTA", 0.1);
+        S.delta2 = delta * delta;
+        const double cmin = env_double("FAST_TAU_SHADOW_COS", 1e-4);
+        S.cos2_min = cmin * cmin;
         S.inner_mode = mixed ? 1 : 0;
     }
     CU(cudaMemcpyAsync(d_jobs, hj, sizeof(Job) * ndirs, cudaMemcpyHostToDevice, st));
@@ -539,34 +552,14 @@ int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64
         else steps = {Step::BI_RESTART, Step::BI1, Step::BI2, Step::BI3};
         status = iterate(E, L, ndirs, d_sc, steps, fn, P.max_iter);
     } else {
+        // FP32 iterations with in-graph FP64 residual replacement: the
+        // replacement slot leads every iteration and is a no-op launch unless
+        // the recursion asked for it.
         launch_counted(FAST_K_INIT64, st, [&] { launch_init64(L, st); });
         std::vector<Step> steps;
-        if (solver == FAST_SOLVER_CG) steps = {Step::CG1, Step::CG2};
-        else steps = {Step::BI_RESTART, Step::BI1, Step::BI2, Step::BI3};
-        const int max_outer = env_int("FAST_TAU_MAX_OUTER", 60);
-        for (int o = 0; o < max_outer && status == FAST_OK; o++) {
-            launch_counted(FAST_K_REFINE, st, [&] { launch_refine(solver == FAST_SOLVER_BICGSTAB, L, st); });
-            CU(cudaMemcpyAsync(hs, d_sc, sizeof(Scalars) * ndirs, cudaMemcpyDeviceToHost, st));
-            CU(cudaStreamSynchronize(st));
-            bool running = false, inner = false;
-            for (int j = 0; j < ndirs; j++) {
-                running |= hs[j].outer_state == RUNNING;
-                inner |= hs[j].state == RUNNING;
-                if (env_int("FAST_TAU_TRACE", 0))
-                    fprintf(stderr,
-                            "trace refine %d job %d outer_state %d state %d relres64 %.3e inner_tol %.3e total_iter %llu "
-                            "rejects %d pending %d\n",
-                            o, j, hs[j].outer_state, hs[j].state,
-                            hs[j].b64_sq > 0 ? std::sqrt(hs[j].r64_sq / hs[j].b64_sq) : 0.0, hs[j].tol,
-                            (unsigned long long)hs[j].total_iter, hs[j].rejects, hs[j].reject_pending);
-            }
-            if (!running) break;
-            // e = 0 for the next inner solve, and for a rejected correction.
-            for (int j = 0; j < ndirs; j++)
-                if (hs[j].outer_state == RUNNING)
-                    CU(cudaMemsetAsync(hj[j].x, 0, (size_t)NP * sizeof(float), st));
-            if (inner) status = iterate(E, L, ndirs, d_sc, steps, dispatch_mixed, P.max_iter);
-        }
+        if (solver == FAST_SOLVER_CG) steps = {Step::REPLACE_CG, Step::CG1, Step::CG2};
+        else steps = {Step::REPLACE_BI, Step::BI1, Step::BI2, Step::BI3};
+        status = iterate(E, L, ndirs, d_sc, steps, dispatch_mixed, P.max_iter);
     }
     if (status == FAST_OK)
         launch_counted(FAST_K_TAU, st, [&] { launch_tau(mixed ? 2 : (prec == FAST_PREC_F32 ? 1 : 0), L, st); });
@@ -596,9 +589,8 @@ int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64
         S.pores = pores;
         fast_tau_result &R = res[j];
         memset(&R, 0, sizeof(R));
-        const int state = mixed ? S.outer_state : S.state;
-        R.status = status_of(state);
-        R.iterations = mixed ? S.total_iter : S.iter;
+        R.status = status_of(S.state);
+        R.iterations = S.iter;
         R.outer_steps = mixed ? (uint32_t)S.outer_steps : 0;
         if (mixed) R.rel_residual = S.b64_sq > 0 ? std::sqrt(S.r64_sq / S.b64_sq) : 0.0;
         else R.rel_residual = S.rhs_sq > 0 ? std::sqrt(S.rsq / S.rhs_sq) : 0.0;

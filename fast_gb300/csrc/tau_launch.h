@@ -6,7 +6,7 @@
 
 namespace ft {
 
-enum class Step { INIT_CG, INIT_BI, CG1, CG2, BI_RESTART, BI1, BI2, BI3 };
+enum class Step { INIT_CG, INIT_BI, CG1, CG2, BI_RESTART, BI1, BI2, BI3, REPLACE_CG, REPLACE_BI };
 
 // Pure-precision solves: `f64` selects double, otherwise float (scalars in
 // the solve precision, as the reference's T).
@@ -14,8 +14,9 @@ void launch_pure_f64(Step s, const Launch &L, cudaStream_t st);
 void launch_pure_f32(Step s, const Launch &L, cudaStream_t st);
 // FP32 inner iterations of a MIXED solve (scalars in double).
 void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st);
-// FP64 refinement step of a MIXED solve.
-void launch_refine(bool bicg, const Launch &L, cudaStream_t st);
+// FP64 residual replacement of a MIXED solve (a no-op launch unless the
+// solve asked for one).
+void launch_replace(bool bicg, const Launch &L, cudaStream_t st);
 void launch_init64(const Launch &L, cudaStream_t st);
 void launch_code(const Launch &L, cudaStream_t st);
 // tau flux sum: src 0 = double x, 1 = float x, 2 = the current FP64 iterate.

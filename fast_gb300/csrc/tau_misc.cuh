@@ -1,64 +1,77 @@
-// FP64 iterative refinement step, tau flux reduction, stencil-code build and
-// porosity count.
+// MIXED FP64 residual replacement, tau flux reduction, stencil-code build
+// and porosity count.
 #pragma once
+#include <type_traits>
 #include "tau_sweep.cuh"
 
 namespace ft {
 
 // ===========================================================================
-// MIXED refinement step (FP64): x64' = x64 + e (e = the FP32 correction of
-// the previous inner solve), r64 = b - A x64' in FP64, and the next inner
-// system A e = fp32(r64) set up with e = 0 and zeroed Krylov vectors.
-// Dots (FP64): |r64|^2, |b|^2, |fp32(r64)|^2, fp32(r64).z.
-// Streams: x64, e, code.
+// MIXED residual replacement (FP64).  The FP32 iterations work on a
+// correction e of the FP64 iterate x64; when one of them asks for it
+// (`replace`), this step folds e into x64 (x64' = x64 + e, e is zeroed by the
+// next step-1 kernel), recomputes the residual b - A x64' in FP64 and hands
+// fp32 of it to the recursion in place of the recursive residual, keeping
+// the Krylov vectors (replace = 1) or restarting them from it (replace = 2,
+// also the first step of a solve).  The true residual decides convergence.
+// Dots, accumulated in FP32 per thread (they steer the iteration and test
+// convergence; they need no more than FP32 accuracy): |fp32(r64)|^2, |b|^2
+// and, for BiCGSTAB, r0.fp32(r64) (r0 = fp32(r64) itself on a restart), for
+// CG fp32(r64).z.  Streams: x64, e, code (+ r0 for BiCGSTAB).
 // ===========================================================================
 template <bool BICG>
-struct OpRefine {
+struct OpReplace {
     using T = double;
-    using SL = Streams<8, 4, 1>;
-    static constexpr int NV = 4;
+    using SL = typename std::conditional<BICG, Streams<8, 4, 1, 4>, Streams<8, 4, 1>>::type;
+    static constexpr int NV = 3;
     using Shared = Coef<float>;
-    struct Vals { double x; float e; uint32_t code; };
-    struct Own { uint32_t code; };
+    struct Vals { double x; float e; uint32_t code; float r0; };
+    struct Own { uint32_t code; float r0; };
     struct Out { double x; float r; };
     const CUtensorMap *tmap[SL::N];
     double *x64n;
-    float *r, *r0, *p0, *v0;
-    Acc<double> a_r64, a_bb, a_r32, a_rz;
+    float *r, *r0, *p, *v;
+    bool restart;
+    Acc<float> a_rr, a_bb, a_d;
 
-    __device__ static bool active(const Scalars &sc) { return sc.outer_state == RUNNING; }
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING && sc.replace != 0; }
     __device__ static void load_shared(Shared &S, const Job &J, int tid) { load_coef<float>(S, J, tid); }
-    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    __device__ static void load2(const unsigned char *st, const Pt &p_, Vals &a, Vals &b)
     {
-        sv2<double, SL, 0>(st, p, a.x, b.x);
-        sv2<float, SL, 1>(st, p, a.e, b.e);
-        load_code2<SL, 2>(st, p, a.code, b.code);
+        sv2<double, SL, 0>(st, p_, a.x, b.x);
+        sv2<float, SL, 1>(st, p_, a.e, b.e);
+        load_code2<SL, 2>(st, p_, a.code, b.code);
+        if constexpr (BICG) sv2<float, SL, 3>(st, p_, a.r0, b.r0);
     }
-    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a)
+    __device__ static void load1(const unsigned char *st, const Pt &p_, Vals &a)
     {
-        a.x = sv<double, SL, 0>(st, p);
-        a.e = sv<float, SL, 1>(st, p);
+        a.x = sv<double, SL, 0>(st, p_);
+        a.e = sv<float, SL, 1>(st, p_);
     }
     __device__ void init(const Job &J, Shared &)
     {
-        const int cur = J.sc->x64_cur;
+        const Scalars &sc = *J.sc;
+        const int cur = sc.x64_cur;
+        const int par = BICG ? (int)(sc.iter & 1) : 0;
         tmap[0] = &J.tm[TM_X64 + cur];
         tmap[1] = &J.tm[TM_X];
         tmap[2] = &J.tm[TM_CODE];
+        if constexpr (BICG) tmap[3] = &J.tm[TM_R0];
         x64n = J.x64[cur ^ 1];
-        r = (float *)J.r[0];
+        r = (float *)J.r[par];
         r0 = (float *)J.r0;
-        p0 = (float *)J.p[0];
-        v0 = (float *)J.v[0];
+        p = (float *)J.p[(int)(sc.iter & 1)];
+        v = BICG ? (float *)J.v[par] : nullptr;
+        restart = sc.replace == 2;
     }
-    __device__ double field(const Geo &, const Coef<double> &, Shared &, const Vals &v, int, int, int) const
+    __device__ double field(const Geo &, const Coef<double> &, Shared &, const Vals &a, int, int, int) const
     {
-        return v.x + (double)v.e;
+        return a.x + (double)a.e;
     }
-    __device__ Own own(const Geo &, const Coef<double> &, Shared &, const Vals &v, int, int, int, double &f) const
+    __device__ Own own(const Geo &, const Coef<double> &, Shared &, const Vals &a, int, int, int, double &f) const
     {
-        f = v.x + (double)v.e;
-        return Own{v.code};
+        f = a.x + (double)a.e;
+        return Own{a.code, a.r0};
     }
     __device__ Out apply(const Geo &g, const Coef<double> &C, Shared &S, const Own &o, int x_, int y_, int z_,
                          double fc, double fxp, double fxm, double fyp, double fym, double fzp, double fzm)
@@ -68,86 +81,73 @@ struct OpRefine {
         const double b = rhs_at<double>(C, g, o.code, x_, y_, z_);
         const double res = b - ax;
         const float r32 = (float)res;
-        const float inv = inv_of<float>(S, g, o.code, x_, y_, z_);
-        a_r64.add_prod(res, res);
-        a_bb.add_prod(b, b);
-        a_r32.add_prod((double)r32, (double)r32);
-        a_rz.add_prod((double)r32, (double)(r32 * inv));
+        const float b32 = (float)b;
+        a_rr.add_prod(r32, r32);
+        a_bb.add_prod(b32, b32);
+        if constexpr (BICG) {
+            a_d.add_prod(restart ? r32 : o.r0, r32);
+        } else {
+            const float inv = inv_of<float>(S, g, o.code, x_, y_, z_);
+            a_d.add_prod(r32, r32 * inv);
+        }
         return Out{fc, r32};
     }
     __device__ void store(int64_t i, const Out &a, const Out &b, bool v0_, bool v1_)
     {
         store2<double>(x64n, i, a.x, b.x, v0_, v1_);
         store2<float>(r, i, a.r, b.r, v0_, v1_);
-        store2<float>(p0, i, 0.f, 0.f, v0_, v1_);
-        if (BICG) {
-            store2<float>(r0, i, a.r, b.r, v0_, v1_);
-            store2<float>(v0, i, 0.f, 0.f, v0_, v1_);
+        if (restart) {
+            store2<float>(p, i, 0.f, 0.f, v0_, v1_);
+            if constexpr (BICG) {
+                store2<float>(r0, i, a.r, b.r, v0_, v1_);
+                store2<float>(v, i, 0.f, 0.f, v0_, v1_);
+            }
         }
     }
-    __device__ void partials(double (&v)[NV]) const
+    __device__ void partials(double (&t)[NV]) const
     {
-        v[0] = a_r64.hi(); v[1] = a_bb.hi(); v[2] = a_r32.hi(); v[3] = a_rz.hi();
+        t[0] = (double)a_rr.hi(); t[1] = (double)a_bb.hi(); t[2] = (double)a_d.hi();
     }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
     {
-        sc.total_iter += sc.iter;
-        sc.iter = 0;
-        sc.state = CONVERGED;  // no inner solve unless set up below
+        const int mode = sc.replace;
+        sc.replace = 0;
         sc.b64_sq = t[1];
-        if (t[1] == 0.0) { sc.outer_state = ZERO_RHS; return; }
-        // Keep a correction only if it lowered the true FP64 residual.  A
-        // rejected one leaves x64 as it was; the host zeroes e and this step
-        // runs again, which re-evaluates x64 and sets up the same inner solve
-        // bit for bit (every reduction has a fixed order).  That replay stops
-        // at the iteration where the rejected solve had its smallest
-        // residual, so it returns the best correction the solve passed by.
-        if (sc.outer_steps > 0 && !sc.reject_pending && !(t[0] < sc.r64_sq)) {
-            sc.rejects += 1;
-            const uint64_t best = sc.iter_min;
-            if (best == 0 || sc.replay_iters != 0 || sc.rejects > 8 || sc.total_iter >= sc.max_total) {
-                sc.outer_state = MAXITER;
-                return;
-            }
-            sc.replay_iters = best;
-            sc.reject_pending = 1;
-            return;
-        }
-        const uint64_t replay = sc.reject_pending ? sc.replay_iters : 0;
-        if (!sc.reject_pending) sc.replay_iters = 0;
-        sc.reject_pending = 0;
+        if (t[1] == 0.0) { sc.state = ZERO_RHS; return; }
         sc.x64_cur ^= 1;
-        sc.r64_sq = t[0];
-        sc.rsq = t[0];
-        if (t[0] <= sc.tol_outer * sc.tol_outer * t[1]) { sc.outer_state = CONVERGED; return; }
-        if (t[0] > sc.div_thresh) { sc.outer_state = DIVERGED; return; }
-        if (sc.total_iter >= sc.max_total) { sc.outer_state = MAXITER; return; }
-        // Ask the FP32 inner solve for the residual reduction still needed
-        // (with a factor 2 margin), but no less than it can deliver.
-        const double rel = sqrt(t[0] / t[1]);
-        double tin = 0.5 * sc.tol_outer / rel;
-        if (tin < sc.inner_floor) tin = sc.inner_floor;
-        if (tin > 0.5) tin = 0.5;
-        sc.tol = tin;
-        sc.rhs_sq = t[2];
-        sc.tol2 = tin * tin * t[2];
-        sc.rsq = t[2];
-        sc.zr = t[3];
-        sc.beta = 0.0;
-        sc.alpha = 1.0;
-        sc.omega = 1.0;
-        sc.rho = t[2];
-        sc.rho_old = 1.0;
-        sc.r0_sq = t[2];
-        if (BICG) sc.beta = t[2];  // (rho/1)*(1/1)
-        sc.restarts = 0;
-        sc.restart = 0;
-        sc.max_iter = sc.max_total - sc.total_iter;
-        if (replay != 0 && replay < sc.max_iter) sc.max_iter = replay;
-        sc.rsq_min = t[2];
-        sc.iter_min = 0;
+        sc.e_reset = 1;
         sc.outer_steps += 1;
-        sc.state = (t[2] > sc.tol2) ? RUNNING : CONVERGED;
+        sc.r64_sq = t[0];
+        const double tol2 = sc.tol_outer * sc.tol_outer * t[1];
+        sc.tol2 = tol2;
+        sc.rhs_sq = t[1];
+        if (t[0] <= tol2) { sc.state = CONVERGED; return; }
+        if (!(t[0] <= sc.div_thresh)) { sc.state = DIVERGED; return; }  // also NaN
+        if (sc.iter >= sc.max_iter) { sc.state = MAXITER; return; }
+        sc.rsq = t[0];
+        sc.rsq_max = t[0];
+        if (mode == 2) {
+            // Fresh Krylov space from the true residual: p (and v) are zero,
+            // so the next step-1 kernel forms p = r (CG: p = z).
+            sc.beta = 0.0;
+            if (BICG) {
+                sc.r0_sq = t[0];
+                sc.rho = t[2];
+                sc.rho_old = 1.0;
+                sc.alpha = 1.0;
+                sc.omega = 1.0;
+            } else {
+                sc.zr = t[2];
+            }
+        } else if (BICG) {
+            // rho_old, alpha and omega are those of the iteration just done.
+            sc.rho = t[2];
+            sc.beta = (t[2] / sc.rho_old) * (sc.alpha / sc.omega);
+        } else {
+            // rho_old holds r.z of the previous iteration (set by CG step 2).
+            sc.beta = t[2] / sc.rho_old;
+            sc.zr = t[2];
+        }
     }
 };
 
@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(NTHREADS) code_kernel(Launch L)
     }
 }
 
-// MIXED: x64[0] = x0 (the reference's initial guess, in FP64), e = 0.
+// MIXED: x64[0] = x0 (the reference's initial guess; its precision does not
+// matter to the converged iterate, so it is formed in FP32), e = 0.
 __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
 {
     __shared__ int s_job;
@@ -245,7 +246,7 @@ __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
         if (!t.v[k]) continue;
         for (int z = t.z0; z < t.z1; ++z) {
             const int64_t i = g.idx(t.gx + k, t.gy, z);
-            x64[i] = x0_at<double>(g, t.gx + k, t.gy, z);
+            x64[i] = (double)x0_at<float>(g, t.gx + k, t.gy, z);
             e[i] = 0.f;
         }
     }
@@ -279,13 +280,13 @@ __global__ void __launch_bounds__(NTHREADS) tau_kernel(Launch L, int use_x64)
             const int64_t i = g.idx(x, t.gy, z);
             const int kn = g.coord(x, t.gy, z) + g.sgn;
             const double here = (double)__ldg(c + i);
-            double prev = 0.0, dx = 0.5;
+            double prev = 0.0, rdx = 2.0;  // 1/dx: dx = 0.5 past the last plane
             if (kn >= 0 && kn < ext) {
                 prev = (double)__ldg(c + i + sstep);
-                dx = 1.0;
+                rdx = 1.0;
             }
             const int self = (__ldg(J.code + i) >> SELF_BIT) & 1;
-            acc.add(cc[self] * (here - prev) / dx);
+            acc.add(cc[self] * (here - prev) * rdx);  // == / dx exactly (dx is 1 or 1/2)
         }
     }
     double v[1] = {acc.hi()};

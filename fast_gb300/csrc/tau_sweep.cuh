@@ -295,7 +295,17 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
     for (; q < NP; ++q) {
         const int zq = pa + q;
         const int st = q % NSTAGE;
+#if FAST_TAU_WAIT_WARP0
+        // Warp 0 waits for the stage; the other warps sleep in the barrier
+        // instead of spinning on the mbarrier, then observe the completed
+        // phase once.
+        if (tid < 32 && !mbar_wait_bounded(smem_u32(&bars[st]), (uint32_t)((q / NSTAGE) & 1))) s_err = 1;
+        __syncthreads();
+        if (s_err) break;
+        if (tid >= 32) (void)mbar_try_wait(smem_u32(&bars[st]), (uint32_t)((q / NSTAGE) & 1));
+#else
         if (!mbar_wait_bounded(smem_u32(&bars[st]), (uint32_t)((q / NSTAGE) & 1))) s_err = 1;
+#endif
         const unsigned char *stage = sbase + st * SB;
         const bool out_plane = zq >= z0 && zq < z1;
         {
@@ -359,7 +369,6 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
             for (int k = q; k < issued; ++k)
                 mbar_wait_bounded(smem_u32(&bars[k % NSTAGE]), (uint32_t)((k / NSTAGE) & 1));
             atomicExch(&J.sc->state, (int32_t)FAULT);
-            atomicExch(&J.sc->outer_state, (int32_t)FAULT);
         }
         return;
     }
@@ -511,6 +520,61 @@ struct OpInit {
 };
 
 // ===========================================================================
+// MIXED iteration control (FP32 vectors, FP64 scalars).  The recursive
+// residual of the FP32 iteration stands for b - A (x64 + e); it is replaced
+// by the true one (OpReplace) once it has fallen by delta below the largest
+// value seen since the last replacement (so the rounding gap between the two,
+// proportional to that largest value, stays small against it), when it
+// claims convergence (the true residual then decides), and with a Krylov
+// restart when the recursion breaks down (BiCGSTAB: r0.r small against
+// |r0||r|, or a non-finite or exploding residual).
+// ===========================================================================
+__device__ __forceinline__ void mixed_request(Scalars &sc, double rsq)
+{
+    if (rsq > sc.rsq_max) sc.rsq_max = rsq;
+    if (rsq <= sc.tol2 || rsq < sc.delta2 * sc.rsq_max) sc.replace = 1;
+    else if (sc.iter >= sc.max_iter) sc.state = MAXITER;
+}
+
+__device__ __forceinline__ void mixed_cg_finish(Scalars &sc, double rsq, double zr_new)
+{
+    sc.rsq = rsq;
+    sc.iter += 1;
+    if (!(rsq <= sc.div_thresh)) {  // non-finite or exploding: restart from the true residual
+        sc.restarts += 1;
+        sc.replace = 2;
+        return;
+    }
+    sc.rho_old = sc.zr;  // r.z of this iteration's start, for a replacement
+    sc.beta = zr_new / sc.zr;
+    sc.zr = zr_new;
+    mixed_request(sc, rsq);
+}
+
+__device__ __forceinline__ void mixed_bicg_finish(Scalars &sc, double r0r, double rsq)
+{
+    sc.rsq = rsq;
+    sc.iter += 1;
+    if (!(rsq <= sc.div_thresh)) {
+        sc.restarts += 1;
+        sc.replace = 2;
+        return;
+    }
+    const double rho_old = sc.rho;
+    sc.rho_old = rho_old;
+    sc.rho = r0r;
+    // The shadow residual r0 has become (numerically) orthogonal to r: in
+    // FP32, r0.r is noise well before |rho| reaches eps^2 |r0|^2.
+    if (fabs(r0r) < sc.eps2 * sc.r0_sq || r0r * r0r < sc.cos2_min * sc.r0_sq * rsq) {
+        sc.restarts += 1;
+        sc.replace = 2;
+        return;
+    }
+    sc.beta = (r0r / rho_old) * (sc.alpha / sc.omega);
+    mixed_request(sc, rsq);
+}
+
+// ===========================================================================
 // CG step 1: p <- z + beta p (z = r/diag on the fly), q = A p, dot p.q.
 // CG.cu:113-135 (z, beta, p update of the previous iteration) + :70-81.
 // Streams: r, p_old, code.
@@ -526,6 +590,7 @@ struct OpCG1 {
     struct Out { T p; };
     const CUtensorMap *tmap[SL::N];
     T *pnew;
+    T *ezero;  // MIXED: e to zero after a residual replacement, else null
     T beta;
     Acc<T> pap;
 
@@ -550,6 +615,7 @@ struct OpCG1 {
         tmap[1] = &J.tm[TM_P + par];
         tmap[2] = &J.tm[TM_CODE];
         pnew = (T *)J.p[par ^ 1];
+        ezero = J.sc->e_reset ? (T *)J.x : nullptr;
         beta = (T)J.sc->beta;
     }
     __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_) const
@@ -573,11 +639,13 @@ struct OpCG1 {
     __device__ void store(int64_t i, const Out &a, const Out &b, bool v0, bool v1)
     {
         store2<T>(pnew, i, a.p, b.p, v0, v1);
+        if (ezero) store2<T>(ezero, i, T(0), T(0), v0, v1);
     }
     __device__ void partials(T (&v)[NV]) const { v[0] = pap.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
     {
         sc.alpha = (double)((ST)sc.zr / (ST)t[0]);  // CG.cu:79-81
+        sc.e_reset = 0;
     }
 };
 
@@ -647,6 +715,10 @@ struct OpCG2 {
     __device__ void partials(T (&v)[NV]) const { v[0] = rr.hi(); v[1] = rz.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
     {
+        if (sc.inner_mode) {
+            mixed_cg_finish(sc, t[0], t[1]);
+            return;
+        }
         const ST rsq = (ST)t[0];
         sc.rsq = rsq;
         if (rsq <= (ST)sc.tol2) {  // CG.cu:108-110: converging iteration not counted
@@ -657,13 +729,6 @@ struct OpCG2 {
         sc.beta = (double)(zr_new / (ST)sc.zr);  // CG.cu:121-123
         sc.zr = zr_new;
         sc.iter += 1;                            // CG.cu:144
-        if (sc.inner_mode) {
-            // FP32 inner solve: remember the best iterate and stop once the
-            // residual has grown well above it; the FP64 refinement decides
-            // what to keep.
-            if (rsq < (ST)sc.rsq_min) { sc.rsq_min = rsq; sc.iter_min = sc.iter; }
-            else if (rsq > (ST)100 * (ST)sc.rsq_min) { sc.state = STALLED; return; }
-        }
         if (rsq > (ST)sc.div_thresh) sc.state = DIVERGED;  // CG.cu:152
         else if (sc.iter >= sc.max_iter) sc.state = MAXITER;
     }
@@ -751,6 +816,7 @@ struct OpBi1 {
     struct Out { T p, v; };
     const CUtensorMap *tmap[SL::N];
     T *pnew, *vnew;
+    T *ezero;  // MIXED: e to zero after a residual replacement, else null
     T beta, nw;
     Acc<T> r0v;
 
@@ -781,6 +847,7 @@ struct OpBi1 {
         tmap[4] = &J.tm[TM_CODE];
         pnew = (T *)J.p[par ^ 1];
         vnew = (T *)J.v[par ^ 1];
+        ezero = J.sc->e_reset ? (T *)J.x : nullptr;
         beta = (T)J.sc->beta;
         nw = (T)(-J.sc->omega);
     }
@@ -808,11 +875,13 @@ struct OpBi1 {
     {
         store2<T>(pnew, i, a.p, b.p, v0, v1);
         store2<T>(vnew, i, a.v, b.v, v0, v1);
+        if (ezero) store2<T>(ezero, i, T(0), T(0), v0, v1);
     }
     __device__ void partials(T (&v)[NV]) const { v[0] = r0v.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
     {
         sc.alpha = (double)((ST)sc.rho / (ST)t[0]);  // BICGSTAB.cu:147
+        sc.e_reset = 0;
     }
 };
 
@@ -968,18 +1037,18 @@ struct OpBi3 {
     __device__ void partials(T (&v_)[NV]) const { v_[0] = r0r.hi(); v_[1] = rr.hi(); }
     __device__ static void finish(Scalars &sc, const double (&t)[NV])
     {
+        if (sc.inner_mode) {
+            mixed_bicg_finish(sc, t[0], t[1]);
+            return;
+        }
         const ST rsq = (ST)t[1];
         sc.rsq = rsq;
         if (rsq > (ST)sc.div_thresh) {  // BICGSTAB.cu:206-209, before ++i
-            sc.state = sc.inner_mode ? STALLED : DIVERGED;
+            sc.state = DIVERGED;
             return;
         }
         sc.iter += 1;  // BICGSTAB.cu:211
         if (!(rsq > (ST)sc.tol2)) { sc.state = CONVERGED; return; }
-        if (sc.inner_mode) {
-            if (rsq < (ST)sc.rsq_min) { sc.rsq_min = rsq; sc.iter_min = sc.iter; }
-            else if (rsq > (ST)100 * (ST)sc.rsq_min) { sc.state = STALLED; return; }
-        }
         if (sc.iter >= sc.max_iter) { sc.state = MAXITER; return; }
         // Loop head of the next iteration (BICGSTAB.cu:95-112).
         const ST rho_old = (ST)sc.rho;
@@ -988,11 +1057,7 @@ struct OpBi3 {
         sc.rho = rho;
         const ST mag = rho < ST(0) ? -rho : rho;
         if (mag < (ST)sc.eps2 * (ST)sc.r0_sq) {
-            // A restart recomputes r = b - A x and takes it as the new shadow
-            // residual.  Inside a MIXED solve that is exactly the next FP64
-            // refinement step, so the inner solve ends here instead.
-            if (sc.inner_mode) sc.state = CONVERGED;
-            else sc.restart = 1;
+            sc.restart = 1;
         } else {
             sc.beta = (double)((rho / rho_old) * ((ST)sc.alpha / (ST)sc.omega));
         }

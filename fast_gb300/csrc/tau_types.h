@@ -30,7 +30,6 @@ enum SolveState : int32_t {
     MAXITER = 2,
     DIVERGED = 3,
     ZERO_RHS = 4,
-    STALLED = 5,   // FP32 inner solve ended because its residual grew
     FAULT = 6,     // a bounded device-side wait ran out (tile loads did not arrive)
 };
 
@@ -54,27 +53,26 @@ struct Scalars {
     double r0_sq;       // BiCGSTAB |r0|^2
     double div_thresh;  // divergence threshold on rsq (1e11 scaled to h=1 units)
     double eps2;        // BiCGSTAB restart threshold eps(T)^2
-    uint64_t iter;      // iterations of the current (inner) solve, reference counting
-    uint64_t max_iter;  // iteration limit of the current (inner) solve
+    uint64_t iter;      // iterations, reference counting
+    uint64_t max_iter;  // iteration limit
     uint64_t restarts;
-    int32_t state;      // SolveState of the current (inner) solve
+    int32_t state;      // SolveState
     int32_t restart;    // BiCGSTAB: restart pending before the next iteration
-    // FP64 iterative refinement (MIXED)
+    // MIXED: FP32 iterations on the correction e of an FP64 iterate x64, with
+    // the recursive residual replaced by fp32(b - A (x64 + e)) computed in
+    // FP64 (x64 += e, e = 0) whenever `replace` is set.
     double tol_outer;   // requested relative tolerance on the FP64 residual
-    double inner_floor; // smallest relative tolerance asked of one FP32 inner solve
-    double r64_sq;      // |b - A x64|^2
+    double r64_sq;      // |b - A x64|^2 at the last replacement
     double b64_sq;      // |b|^2 in FP64
-    uint64_t total_iter;    // inner iterations summed over refinement steps
-    uint64_t max_total;     // limit on total_iter
-    int32_t outer_state;    // SolveState of the refinement loop
-    int32_t outer_steps;
+    double rsq_max;     // largest recursive |r|^2 since the last replacement
+    double delta2;      // replace once |r|^2 < delta2 * rsq_max
+    double cos2_min;    // BiCGSTAB: restart once (r0.r)^2 < cos2_min |r0|^2 |r|^2
+    int32_t replace;    // 0: none pending, 1: residual replacement, 2: replacement + Krylov restart
+    int32_t e_reset;    // 1: the next step-1 kernel zeroes e
+    int32_t outer_steps;    // residual replacements done
     int32_t x64_cur;        // which x64 buffer holds the current iterate
-    int32_t inner_mode;     // 1: FP32 inner solve of a MIXED solve
-    double rsq_min;         // smallest inner |r|^2 seen (growth guard)
-    uint64_t iter_min;      // inner iterations completed when rsq_min was reached
-    uint64_t replay_iters;  // >0: stop the next inner solve after this many iterations
-    int32_t rejects;        // refinement steps whose correction was rejected
-    int32_t reject_pending; // 1: the last correction was rejected; e must be zeroed and x64 re-evaluated
+    int32_t inner_mode;     // 1: MIXED solve
+    int32_t pad1;
     // reductions for tau and porosity
     double flux_sum;    // sum over voxels of the tau flux term
     uint64_t pores;     // number of zero (pore) voxels

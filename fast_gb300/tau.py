@@ -56,8 +56,9 @@ DSOLVER_CG = DiffusionSolverType.DSOLVER_CG
 
 
 class Precision(IntEnum):
-    """F64/F32: the reference's `-p double` / `-p float`; MIXED: FP32 inner
-    iterations inside FP64 iterative refinement."""
+    """F64/F32: the reference's `-p double` / `-p float`; MIXED: FP32 Krylov
+    iterations on a correction of an FP64 iterate, with FP64 true-residual
+    replacement and an FP64 convergence test."""
     F64 = 0
     F32 = 1
     MIXED = 2

@@ -57,9 +57,13 @@ typedef enum fast_solver { FAST_SOLVER_BICGSTAB = 0, FAST_SOLVER_CG = 1 } fast_s
 
 /* Arithmetic of the solve.  F64 / F32 are the reference's `-p double` /
  * `-p float` (TauModule.h:19,125-129): the whole solve in that type.  MIXED is
- * the engine's fast path: FP32 inner iterations with compensated dot
- * products inside an FP64 iterative-refinement loop whose true residual
- * b - A x, correction update of x and tau integral are FP64. */
+ * the engine's fast path: FP32 Krylov iterations (FP32-accumulated,
+ * block-compensated dot products) on a correction e of an FP64 iterate x;
+ * whenever the FP32 recursive residual has fallen a decade, claims
+ * convergence or breaks down, an FP64 step folds e into x, recomputes the true
+ * residual b - A x in FP64 and hands it back to the recursion (residual
+ * replacement, with a Krylov restart on breakdown).  Convergence is decided
+ * on the FP64 true residual; the tau flux integral is FP64. */
 typedef enum fast_precision { FAST_PREC_F64 = 0, FAST_PREC_F32 = 1, FAST_PREC_MIXED = 2 } fast_precision;
 
 /* Face diffusivity between two voxels.  The reference uses the arithmetic
@@ -74,7 +78,7 @@ typedef struct fast_tau_params {
     int32_t precision;      /* fast_precision */
     int32_t face_mean;      /* fast_face_mean; 0 = arithmetic */
     double tolerance;       /* relative residual, reference default 1e-6 */
-    uint64_t max_iter;      /* reference default 10000; MIXED: cap on total inner iterations */
+    uint64_t max_iter;      /* reference default 10000; MIXED: cap on the FP32 iterations */
     double d0;              /* pore diffusivity; the reference passes float 1.0 */
     double d1;              /* solid diffusivity; the reference passes (double)0.001f */
     double porosity;        /* < 0: computed on the GPU (getPorosity<T>); else used as given */
@@ -93,8 +97,9 @@ typedef struct fast_tau_result {
     double rel_residual;    /* |r|/|b| at exit (recursive residual; MIXED: true FP64 residual) */
     uint64_t iterations;    /* reference counting: CG excludes the converging iteration,
                                BiCGSTAB counts it (CG.cu:109-144, BICGSTAB.cu:211);
-                               MIXED: total inner iterations over all refinement steps */
-    uint32_t outer_steps;   /* MIXED: refinement steps (0 otherwise) */
+                               MIXED: FP32 iterations */
+    uint32_t outer_steps;   /* MIXED: FP64 residual replacements, the first (x = x0) included;
+                               0 otherwise */
     int32_t status;         /* fast_status */
 } fast_tau_result;
 
@@ -138,7 +143,7 @@ FAST_API int fast_porosity(const uint8_t *mask, int64_t nx, int64_t ny, int64_t 
 /* Kernel kinds of fast_tau_stats. */
 enum {
     FAST_K_CODE = 0, FAST_K_INIT = 1, FAST_K_CG1 = 2, FAST_K_CG2 = 3, FAST_K_BI_RESTART = 4,
-    FAST_K_BI1 = 5, FAST_K_BI2 = 6, FAST_K_BI3 = 7, FAST_K_REFINE = 8, FAST_K_INIT64 = 9,
+    FAST_K_BI1 = 5, FAST_K_BI2 = 6, FAST_K_BI3 = 7, FAST_K_REPLACE = 8, FAST_K_INIT64 = 9,
     FAST_K_TAU = 10, FAST_K_COUNT = 16
 };
 
@@ -167,6 +172,37 @@ FAST_API int fast_tau_last_stats(fast_tau_stats *out);
  * stream; the call synchronises it.  porosity is nullable. */
 FAST_API int fast_porosity_device_noalloc(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz,
                                           uint64_t *pore_count, double *porosity, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Connected components (the reachability pre-pass)                         */
+/* ------------------------------------------------------------------------ */
+
+/* getVolumeCCL(mask, background) (fastlib/src/volume/VolumeSegmentation.cpp:
+ * 33-64) = VolumeCCL_Label + VolumeCCL_BoundaryLabels (fastlib/src/cuda/
+ * VolumeCCL.cu:381-620, 753-818), on the GPU, with the reference's numbering:
+ * foreground = voxels != background, 6-connected; labels[i] = 0 for
+ * background, else 1..K with components ordered by their smallest linear
+ * index (x fastest); *num_labels = K + 1.  boundary (nullable, host,
+ * boundary_cap bytes, needs 7 * num_labels): row d (Dir order; X_POS is the
+ * x = nx-1 face) marks labels touching face d, row 6 is the AND of rows 0-5
+ * (VolumeCCL::getDirMask).  A too small boundary buffer gives FAST_BAD_ARG
+ * with *num_labels set.  labels (host, nx*ny*nz uint32) is nullable.  Volumes
+ * of 4294967295 voxels or more are rejected. */
+FAST_API int fast_ccl_label(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, uint8_t background,
+                            uint32_t *labels, uint32_t *num_labels, uint8_t *boundary, uint64_t boundary_cap);
+
+/* The same on a DEVICE mask, labels written to DEVICE memory d_labels
+ * (nx*ny*nz uint32); boundary stays a host buffer.  stream: a cudaStream_t
+ * as void*, NULL = the legacy default stream; the call synchronises it. */
+FAST_API int fast_ccl_label_device(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, uint8_t background,
+                                   uint32_t *d_labels, uint32_t *num_labels, uint8_t *boundary,
+                                   uint64_t boundary_cap, void *stream);
+
+/* VolumeCCL_BoundaryLabels (fastlib/src/cuda/VolumeCCL.cu:753-818) alone, on
+ * DEVICE labels from fast_ccl_label_device: boundary (host, 7 * num_labels
+ * bytes) as fast_ccl_label fills it. */
+FAST_API int fast_ccl_boundary_device(const uint32_t *d_labels, int64_t nx, int64_t ny, int64_t nz,
+                                      uint32_t num_labels, uint8_t *boundary, void *stream);
 
 /* Message of the calling thread's last failure ("" if none). */
 FAST_API const char *fast_last_error(void);

@@ -17,7 +17,7 @@ the same numbers:
                     for the benchmark volumes (64^3 spheres; 256^3 ellipsoids,
                     three directions).
 
-Usage:  python tests/golden/make_golden.py [small|workloads|all]
+Usage:  python tests/golden/make_golden.py [small|workloads|bicgstab1e-7|all]
 """
 import hashlib
 import json
@@ -162,9 +162,37 @@ def workloads():
             json.dump(dict(generator="tests/golden/make_golden.py", workloads=out), f, indent=1)
 
 
+def workloads_bicgstab_1e7():
+    """Adds FP64 BiCGSTAB (the GPU path's and Eigen's recurrences) at tol 1e-7 (the tolerance at
+    which BiCGSTAB meets |dtau|/tau <= 1e-5 on the 256^3 workload) to
+    workloads.json."""
+    path = os.path.join(HERE, "workloads.json")
+    with open(path) as f:
+        doc = json.load(f)
+    for name, e in doc["workloads"].items():
+        spec = e["spec"]
+        if spec["kind"] == "spheres":
+            m = volumes.spheres(spec["shape"], spec["seed"], spec["r"], spec["r"], spec["frac"])
+        else:
+            m = volumes.ellipsoids(spec["shape"], spec["seed"], spec["a"], spec["aspect"], spec["frac"])
+        assert sha(m) == e["sha256"]
+        for d, rec in e["dirs"].items():
+            r = O.get_tortuosity(m, dir=int(d), solver=O.BICGSTAB, tol=1e-7, max_iter=100000)
+            rec["tau_bicgstab_1e-7"] = r["tau"]
+            rec["iters_bicgstab_1e-7"] = r["iters"]
+            re_ = O.get_tortuosity(m, dir=int(d), solver=O.BICGSTAB, tol=1e-7, max_iter=100000, variant=O.EIGEN)
+            rec["tau_bicgstab_eigen_1e-7"] = re_["tau"]
+            rec["iters_bicgstab_eigen_1e-7"] = re_["iters"]
+            print(name, d, r["tau"], r["iters"], re_["tau"], re_["iters"], flush=True)
+    with open(path, "w") as f:
+        json.dump(doc, f, indent=1)
+
+
 if __name__ == "__main__":
     what = sys.argv[1] if len(sys.argv) > 1 else "all"
     if what in ("small", "all"):
         small_cases()
     if what in ("workloads", "all"):
         workloads()
+    if what in ("bicgstab1e-7", "all"):
+        workloads_bicgstab_1e7()

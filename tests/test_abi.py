@@ -90,3 +90,17 @@ def test_benchmark_volume_hash(native):
     s = w["spec"]
     m = volumes.spheres(tuple(s["shape"]), s["seed"], s["r"], s["r"], s["frac"])
     assert hashlib.sha256(m.tobytes()).hexdigest() == w["sha256"]
+
+
+def test_ccl_argument_errors_without_gpu(native):
+    """The labelling entry points check their arguments before any CUDA call."""
+    n = C.c_uint32(0)
+    assert native.fast_ccl_label(None, 4, 4, 4, 255, None, C.byref(n), None, 0) == 2
+    m = np.zeros((4, 4, 4), np.uint8)
+    mp = m.ctypes.data_as(C.c_void_p)
+    assert native.fast_ccl_label(mp, 0, 4, 4, 255, None, C.byref(n), None, 0) == 8
+    assert native.fast_ccl_label(mp, 4096, 4096, 256, 255, None, C.byref(n), None, 0) == 8
+    assert b"4294967294" in native.fast_last_error()
+    assert native.fast_ccl_label(mp, 4, 4, 4, 255, None, None, None, 0) == 8
+    assert native.fast_ccl_label_device(None, 4, 4, 4, 255, None, C.byref(n), None, 0, None) == 8
+    assert native.fast_ccl_boundary_device(None, 4, 4, 4, 3, None, None) == 8

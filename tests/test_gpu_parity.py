@@ -8,8 +8,10 @@ Tolerances:
     runs stop at different iterates of equal residual: |dtau|/tau <= 1e-8 at
     tol 1e-10 and <= 1e-5 at tol 1e-6; iteration counts within 50 %.
   * F32 vs the float oracle at tol 1e-5: |dtau|/tau <= 1e-4.
-  * MIXED (FP32 inner + FP64 refinement) at tol 1e-7 vs the FP64 oracle at
-    tol 1e-10: |dtau|/tau <= 1e-5 (the engine's accuracy contract).  A
+  * MIXED (FP32 iterations + FP64 residual replacement) at tol 1e-7 vs the
+    FP64 oracle at tol 1e-10: |dtau|/tau <= 1e-5 (the engine's accuracy
+    contract); at tol 1e-10, far below what FP32 alone can reach, within 1e-8
+    (the FP64 residual replacement carries the solve there).  A
     relative residual of 1e-6 is not enough for 1e-5 in tau on contrast-1000
     media: the reference's own FP64 BiCGSTAB at tol 1e-6 misses it by 3x on
     the 256^3 benchmark volume.
@@ -86,6 +88,31 @@ def test_mixed_within_1e5_of_fp64_oracle(gpu, oracle, solver):
         tau = ft.get_tortuosity(mask, p, solver)
         ref = oracle.get_tortuosity(mask, dir=d, solver=1, tol=1e-10)
         assert rel(tau, ref["tau"]) <= 1e-5, (d, tau, ref["tau"])
+
+
+@pytest.mark.parametrize("solver", [ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB])
+def test_mixed_reaches_fp64_accuracy(gpu, oracle, solver):
+    mask = _vol((40, 36, 44), seed=21, frac=0.55, r=3.5)
+    for d in (1, 2, 5):
+        p = ft.TortuosityParams(dir=ft.Dir(d), tolerance=1e-10, precision=ft.Precision.MIXED)
+        res = ft.solve_directions(mask, [ft.Dir(d)], p, solver)[0]
+        assert res.status == ft.Status.OK, res
+        assert res.rel_residual <= 1e-10
+        assert res.outer_steps >= 2  # the FP64 replacement ran beyond the first setup
+        ref = oracle.get_tortuosity(mask, dir=d, solver=1, tol=1e-10)
+        assert rel(res.tau, ref["tau"]) <= 1e-8, (d, res.tau, ref["tau"])
+
+
+def test_mixed_multi_direction_equals_single(gpu):
+    mask = _vol((30, 26, 34), seed=23, frac=0.5, r=3.0)
+    dirs = [ft.Dir.X_POS, ft.Dir.Y_NEG, ft.Dir.Z_POS]
+    for solver in (ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB):
+        p = ft.TortuosityParams(tolerance=1e-8, precision=ft.Precision.MIXED)
+        multi = ft.solve_directions(mask, dirs, p, solver)
+        for d, r in zip(dirs, multi):
+            single = ft.solve_directions(mask, [d], p, solver)[0]
+            # the right-hand sides of one launch never interact: bit-identical
+            assert (r.tau, r.iterations, r.outer_steps) == (single.tau, single.iterations, single.outer_steps)
 
 
 def test_known_answers(gpu):
