@@ -381,9 +381,11 @@ def run_ours(args, ws, rank, local):
 
 
 C_RESULT_BYTES = 40  # sizeof(fast_tau_result)
-# DRAM bytes per launch of the dominant kernel from one ncu capture
-# (profiles/), null until captured.
-NCU_TRAFFIC = {}
+# DRAM bytes (read + write) per bench launch of each kernel, from one ncu
+# --set full capture of a one-direction launch of the same volume
+# (profiles/bi1_bi3_ellipsoids256_x_full.md), scaled by 3 to the three
+# right-hand sides a bench launch processes (traffic grows with the voxels).
+NCU_TRAFFIC = {"bi1": 3 * 415.2e6, "bi3": 3 * 518.7e6}
 
 
 def run_ncu_case(args):

@@ -27,7 +27,7 @@ CASES = [
     ("line_x", lambda: _random((1, 1, 97), 0.6, 6)),
     ("line_z", lambda: _random((97, 1, 1), 0.6, 7)),
     ("plane_xy", lambda: _random((1, 45, 45), 0.55, 8)),
-    ("checker", lambda: (((np.indices((8, 9, 10)).sum(0) % 2) * 255).astype(np.uint8)),  # K = N/2 singletons
+    ("checker", lambda: ((np.indices((8, 9, 10)).sum(0) % 2) * 255).astype(np.uint8)),  # K = N/2 singletons
 ]
 
 
@@ -83,7 +83,7 @@ def test_device_entry_matches_host(gpu):
 
 def test_many_components_boundary_retry(gpu, oracle):
     # more components than the first boundary buffer guess forces the retry
-    m = (((np.indices((64, 128, 260)).sum(0) % 2) * 255).astype(np.uint8))
+    m = ((np.indices((64, 128, 260)).sum(0) % 2) * 255).astype(np.uint8)
     c = ccl.get_volume_ccl(m)
     assert c.num_labels == (m == 0).sum() + 1 > (1 << 20)
     ref_labels, ref_n = oracle.ccl_label(m)
