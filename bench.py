@@ -388,6 +388,296 @@ C_RESULT_BYTES = 40  # sizeof(fast_tau_result)
 NCU_TRAFFIC = {"bi1": 3 * 415.2e6, "bi3": 3 * 518.7e6}
 
 
+# ---------------------------------------------------------------------------
+# Other configurations of the workload table (each prints its own JSON line)
+# ---------------------------------------------------------------------------
+def _line(metric, value, unit, args, ms_per_step, dtype, config, **extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+         "dtype": dtype, "data": "synthetic (seeded generator stand-ins)", "config": config}
+    d.update(extra)
+    return d
+
+
+def _events(stream):
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def run_c1(args):
+    """Plain drop-in: 64^3 spheres (seed 0, r = 5, solid 0.60), direction x,
+    Jacobi-PCG, tol 1e-6, FP64, through fast_tau_solve with a host mask (the
+    getTortuosity<double> replacement), one solve per step; tau compared with
+    the oracle's Eigen CG (the reference --cpu path) on the same volume."""
+    import torch
+    import fast_gb300 as ft
+    from fast_gb300 import volumes
+    from oracle import oracle as O
+    m = volumes.spheres((64, 64, 64), seed=0, r_min=5.0, solid_fraction=0.60)
+    p = ft.TortuosityParams(dir=ft.Dir.X_POS, tolerance=1e-6, max_iter=10000, precision=ft.Precision.F64)
+    for _ in range(args.warmup):
+        ft.get_tortuosity(m, p, ft.DSOLVER_CG)
+    lat = []
+    it = [0]
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        tau = ft.get_tortuosity(m, p, ft.DSOLVER_CG, iterations_out=it)
+        lat.append(time.perf_counter() - t0)
+    O.build()
+    t0 = time.perf_counter()
+    ref = O.get_tortuosity(m, dir=0, solver=O.CG, tol=1e-6, max_iter=10000, variant=O.EIGEN)
+    t_cpu = time.perf_counter() - t0
+    w = json.load(open(os.path.join(ROOT, "tests", "golden", "workloads.json")))["workloads"]["spheres64"]
+    exact = w["dirs"]["0"]["tau_cg_1e-10"]
+    mean = statistics.mean(lat)
+    line = _line("tau solves/s", 1.0 / mean, "solves/s", args, mean * 1e3, "f64",
+                 {"workload": "c1_spheres64_x_cg_f64_dropin", "volume": "64^3 spheres seed 0 r=5 solid 0.60",
+                  "solver": "Jacobi-PCG", "tol": 1e-6, "api": "fast_tau_solve (host mask, synchronous)"},
+                 tau=tau, iterations=it[0], latency_ms={"p50": 1e3 * statistics.median(lat), "max": 1e3 * max(lat)},
+                 tau_cpu_eigen=ref["tau"], iterations_cpu_eigen=ref["iters"],
+                 dtau_rel_vs_cpu_eigen=abs(tau - ref["tau"]) / ref["tau"],
+                 dtau_rel_vs_fp64_oracle_1e10=abs(tau - exact) / exact,
+                 cpu_baseline={"value": 1.0 / t_cpu, "unit": "solves/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": "oracle FP64 Eigen-recurrence CG, full solve of the same "
+                                                         "volume (assembly + solve + tau)"},
+                 e2e={"value": 1.0 / mean, "unit": "solves/s", "h2d_bytes_per_step": int(m.size),
+                      "d2h_bytes_per_step": 40})
+    print(json.dumps(line), flush=True)
+
+
+def c3_volumes():
+    """64 volumes, seeds 100-163: each dimension uniform in 64..192, sphere
+    radius uniform 3..8 voxels, solid fraction uniform 0.40..0.75, direction
+    uniform over x, y, z."""
+    from concurrent.futures import ThreadPoolExecutor
+    from fast_gb300 import volumes
+    specs = []
+    for seed in range(100, 164):
+        rng = np.random.default_rng(seed)
+        shape = tuple(int(v) for v in rng.integers(64, 193, size=3))
+        frac = float(rng.uniform(0.40, 0.75))
+        d = int(rng.choice([0, 2, 4]))
+        specs.append((shape, seed, frac, d))
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        masks = list(ex.map(lambda s: volumes.spheres(s[0], seed=s[1], r_min=3.0, r_max=8.0, solid_fraction=s[2]),
+                            specs))
+    return [(m, s[3]) for m, s in zip(masks, specs)]
+
+
+def run_c3(args):
+    """Batched launch: the 64 uneven volumes of c3_volumes() solved together
+    (fast_tau_solve_batch_device, MIXED PCG, tol 1e-6), against the plain
+    drop-in solver (FP64, one volume per call) and MIXED one per call on the
+    same volumes; |dtau|/tau against FP64 PCG at tol 1e-10 (batched)."""
+    import torch
+    import fast_gb300 as ft
+    from fast_gb300 import _native
+    vols = c3_volumes()
+    d_masks = [torch.from_numpy(m).cuda() for m, _ in vols]
+    spec = [(t.data_ptr(), m.shape, d) for t, (m, d) in zip(d_masks, vols)]
+    stream = torch.cuda.current_stream()
+    p = ft.TortuosityParams(tolerance=1e-6, max_iter=10000, precision=ft.Precision.MIXED)
+    for _ in range(args.warmup):
+        res = ft.solve_batch_device(spec, p, ft.DSOLVER_CG, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = _events(stream)
+    launches = 0
+    e0.record(stream)
+    for _ in range(args.steps):
+        res = ft.solve_batch_device(spec, p, ft.DSOLVER_CG, stream=stream.cuda_stream)
+        launches += _native.last_stats()["launches"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    value = len(vols) / (ms / 1e3)
+
+    def one_at_a_time(prec, n):
+        q = ft.TortuosityParams(tolerance=1e-6, max_iter=10000, precision=prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for (ptr, shape, d) in spec[:n]:
+            ft.solve_directions_device(ptr, shape, [ft.Dir(d)], q, ft.DSOLVER_CG, stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        return n / (time.perf_counter() - t0)
+
+    plain_f64 = one_at_a_time(ft.Precision.F64, len(vols))
+    plain_mixed = one_at_a_time(ft.Precision.MIXED, len(vols))
+    ref = ft.solve_batch_device(spec, ft.TortuosityParams(tolerance=1e-10, max_iter=100000,
+                                                          precision=ft.Precision.F64), ft.DSOLVER_CG,
+                                stream=stream.cuda_stream)
+    dt = [abs(a.tau - b.tau) / b.tau for a, b in zip(res, ref)]
+    voxels = sum(m.size for m, _ in vols)
+    line = _line("tau solves/s", value, "solves/s", args, ms, "f32+f64",
+                 {"workload": "c3_batch64_uneven_cg_mixed", "volumes": "64, seeds 100-163, dims U[64,192], "
+                  "sphere r U[3,8], solid U[0.40,0.75], dir U{x,y,z}", "solver": "Jacobi-PCG", "tol": 1e-6,
+                  "api": "fast_tau_solve_batch_device (one launch per solver step over all volumes, "
+                         "16-iteration CUDA graphs)"},
+                 voxels=int(voxels), all_converged=all(r.status == ft.Status.OK for r in res),
+                 iterations={"min": min(r.iterations for r in res), "max": max(r.iterations for r in res)},
+                 plain_dropin_f64_solves_per_s=plain_f64, plain_mixed_solves_per_s=plain_mixed,
+                 speedup_vs_plain_f64=value / plain_f64, speedup_vs_plain_mixed=value / plain_mixed,
+                 dtau_rel_vs_fp64_1e10={"max": max(dt), "median": statistics.median(dt)},
+                 gpu_launches_per_step=launches / max(args.steps, 1))
+    print(json.dumps(line), flush=True)
+
+
+def c4_requests(n, seed=2024):
+    """Serving stream requests: edge log-uniform in [32, 384] (cubic),
+    spheres (r U[3,8]) or ellipsoids (semi-major 8, aspect U[0.1,1.0]),
+    solid fraction U[0.40,0.75], direction uniform over the six, CG or
+    BiCGSTAB."""
+    from concurrent.futures import ThreadPoolExecutor
+    from fast_gb300 import volumes
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(n):
+        e = int(round(float(np.exp(rng.uniform(np.log(32), np.log(384))))))
+        frac = float(rng.uniform(0.40, 0.75))
+        kind = "spheres" if rng.random() < 0.5 else "ellipsoids"
+        aspect = float(rng.uniform(0.1, 1.0))
+        specs.append(dict(edge=e, frac=frac, kind=kind, aspect=aspect, seed=int(rng.integers(1 << 30)),
+                          dir=int(rng.integers(6)), solver=int(rng.integers(2))))
+
+    def gen(sp):
+        sh = (sp["edge"],) * 3
+        if sp["kind"] == "spheres":
+            return volumes.spheres(sh, seed=sp["seed"], r_min=3.0, r_max=8.0, solid_fraction=sp["frac"])
+        return volumes.ellipsoids(sh, sp["seed"], 8.0, sp["aspect"], sp["frac"])
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        masks = list(ex.map(gen, specs))
+    return specs, masks
+
+
+def run_c4(args):
+    """Serving stream: Poisson arrivals of c4_requests() at each rate of
+    --rates into one TauServer (MIXED, tol 1e-6); latency = completion minus
+    arrival; against the plain drop-in solver (FP64, one request per call,
+    back to back) on the same requests."""
+    import torch
+    import fast_gb300 as ft
+    from fast_gb300.serve import TauServer
+    specs, masks = c4_requests(args.requests)
+    out = {}
+    rng = np.random.default_rng(7)
+    for rate in args.rates:
+        gaps = rng.exponential(1.0 / rate, size=len(masks))
+        arrivals = np.cumsum(gaps)
+        with TauServer(tolerance=1e-6, chunk=16) as srv:
+            t0 = srv.now()
+            k = 0
+            done = []
+            while k < len(masks) or srv.busy():
+                now = srv.now() - t0
+                while k < len(masks) and arrivals[k] <= now:
+                    srv.submit(masks[k], ft.Dir(specs[k]["dir"]), ft.DiffusionSolverType(specs[k]["solver"]))
+                    k += 1
+                if srv.busy():
+                    done.extend(srv.poll())
+                elif k < len(masks):
+                    time.sleep(max(0.0, min(0.01, arrivals[k] - (srv.now() - t0))))
+            span = max(c.t_done for c in done) - (t0 + arrivals[0])
+        by_ticket = sorted(done, key=lambda c: c.ticket)
+        lat = [c.t_done - (t0 + arrivals[i]) for i, c in enumerate(by_ticket)]
+        out[str(rate)] = {"solves_per_s": len(done) / span, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                          "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                          "all_converged": all(c.result.status == ft.Status.OK for c in done)}
+    # plain drop-in, one request per call (a bounded sample of the same stream)
+    nplain = min(len(masks), args.plain_sample)
+    q = {s: ft.TortuosityParams(tolerance=1e-6, precision=ft.Precision.F64) for s in (0, 1)}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(nplain):
+        ft.solve_directions(masks[k], [ft.Dir(specs[k]["dir"])], q[specs[k]["solver"]],
+                            ft.DiffusionSolverType(specs[k]["solver"]))
+    plain = nplain / (time.perf_counter() - t0)
+    best = max(v["solves_per_s"] for v in out.values())
+    voxels = [m.size for m in masks]
+    line = _line("tau solves/s", best, "solves/s", args, 1e3 / best, "f32+f64",
+                 {"workload": "c4_serving_stream", "requests": len(masks),
+                  "mix": "edge log-U[32,384] cubic, spheres r U[3,8] or ellipsoids aspect U[0.1,1], "
+                         "solid U[0.40,0.75], dir U(6), CG or BiCGSTAB", "tol": 1e-6,
+                  "server": "TauServer MIXED, 16-iteration chunks, admission by HBM footprint"},
+                 rates=out, plain_dropin_f64_solves_per_s=plain, plain_sample=nplain,
+                 speedup_vs_plain_f64=best / plain,
+                 voxels_per_request={"mean": float(np.mean(voxels)), "max": int(max(voxels))})
+    print(json.dumps(line), flush=True)
+
+
+def run_c5(args):
+    """Large volume: 1024^3 spheres (seed 7, r = 10, solid 0.65); GPU CCL of
+    the pore phase (label count, components spanning x, canonical-order check
+    of the labels on the device), then MIXED Jacobi-PCG in x to tol 1e-6,
+    reported as algorithmic GB/s (25 B per voxel-iteration) against the
+    measured HBM peak; tau compared with a MIXED solve to tol 1e-9."""
+    import torch
+    import fast_gb300 as ft
+    from fast_gb300 import _native, ccl, volumes
+    n = args.c5_edge
+    t0 = time.perf_counter()
+    m = volumes.spheres((n, n, n), seed=7, r_min=10.0, solid_fraction=0.65)
+    t_gen = time.perf_counter() - t0
+    d_mask = torch.from_numpy(m).cuda()
+    del m
+    stream = torch.cuda.current_stream()
+    d_labels = torch.empty((n, n, n), dtype=torch.int32, device="cuda")
+    ccl.get_volume_ccl_device(d_mask.data_ptr(), (n, n, n), d_labels.data_ptr(), background=255, boundary=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    c = ccl.get_volume_ccl_device(d_mask.data_ptr(), (n, n, n), d_labels.data_ptr(), background=255)
+    torch.cuda.synchronize()
+    t_ccl = time.perf_counter() - t0
+    lab = d_labels.view(-1)
+    # canonical numbering: first occurrence of label k+1 after that of label k
+    fg = lab != 0
+    first = torch.full((c.num_labels,), lab.numel(), dtype=torch.int64, device="cuda")
+    idx = torch.nonzero(fg).squeeze(1)
+    first.scatter_reduce_(0, lab[idx].long(), idx, reduce="amin")
+    canonical = bool((first[2:] > first[1:-1]).all().item()) if c.num_labels > 2 else True
+    spanning = c.get_dir_mask(ft.Dir.X_NEG, ft.Dir.X_POS)
+    pores = int(fg.sum().item())
+    sizes = torch.bincount(lab.long(), minlength=c.num_labels)
+    span_vox = int(sizes[torch.from_numpy(spanning.astype(bool)).cuda()].sum().item())
+    del first, idx, fg, sizes, lab, d_labels
+    torch.cuda.empty_cache()
+
+    p = ft.TortuosityParams(tolerance=1e-6, max_iter=100000, precision=ft.Precision.MIXED)
+    e0, e1 = _events(stream)
+    e0.record(stream)
+    res = ft.solve_directions_device(d_mask.data_ptr(), (n, n, n), [ft.Dir.X_POS], p, ft.DSOLVER_CG,
+                                     stream=stream.cuda_stream)[0]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    pp = ft.TortuosityParams(tolerance=1e-6, max_iter=100000, precision=ft.Precision.MIXED, profile=True)
+    ft.solve_directions_device(d_mask.data_ptr(), (n, n, n), [ft.Dir.X_POS], pp, ft.DSOLVER_CG,
+                               stream=stream.cuda_stream)
+    prof = _native.last_stats()["kernels"]
+    N = n ** 3
+    iter_ms = sum(prof.get(k, {"ms": 0})["ms"] for k in ("cg1", "cg2", "replace"))
+    gbs = 25.0 * N * res.iterations / (iter_ms / 1e3) / 1e9
+    peak, kind = load_peaks()
+    ref = None
+    if not args.c5_no_reference:
+        q = ft.TortuosityParams(tolerance=1e-9, max_iter=200000, precision=ft.Precision.MIXED)
+        ref = ft.solve_directions_device(d_mask.data_ptr(), (n, n, n), [ft.Dir.X_POS], q, ft.DSOLVER_CG,
+                                         stream=stream.cuda_stream)[0]
+    line = _line("tau solves/s", 1e3 / ms, "solves/s", args, ms, "f32+f64",
+                 {"workload": f"c5_spheres{n}_x_cg_mixed", "volume": f"{n}^3 spheres seed 7 r=10 solid 0.65",
+                  "solver": "Jacobi-PCG", "tol": 1e-6},
+                 tau=res.tau, iterations=res.iterations, status=int(res.status),
+                 stencil_iteration={"gbs_at_25B": gbs, "peak": peak, "peak_kind": kind, "frac": gbs / peak,
+                                    "frac_of_8000": gbs / 8000.0,
+                                    "kernel_ms": {k: round(v["ms"], 2) for k, v in prof.items()}},
+                 ccl={"seconds": t_ccl, "num_labels": c.num_labels, "canonical_order": canonical,
+                      "pore_voxels": pores, "x_spanning_components": int(spanning[1:].sum()),
+                      "x_spanning_pore_fraction": span_vox / max(pores, 1)},
+                 generation_seconds=t_gen,
+                 tau_ref_mixed_1e9=(ref.tau if ref else None),
+                 dtau_rel_vs_1e9=(abs(res.tau - ref.tau) / ref.tau if ref else None),
+                 ref_iterations=(ref.iterations if ref else None))
+    print(json.dumps(line), flush=True)
+
+
 def run_ncu_case(args):
     """A short, fixed run of the workload's kernels for profiler captures:
     the bench volume, one direction (x), MIXED BiCGSTAB stopped after
@@ -414,11 +704,25 @@ def main():
     ap.add_argument("--ncu-case", action="store_true",
                     help="run a short fixed slice of the workload for profiler captures and exit")
     ap.add_argument("--ncu-iters", type=int, default=12)
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c2 (default) is the headline; the others print their own line")
+    ap.add_argument("--requests", type=int, default=64, help="c4: requests in the stream")
+    ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 2000.0], help="c4: arrival rates (1/s)")
+    ap.add_argument("--plain-sample", type=int, default=16, help="c4: requests timed on the plain solver")
+    ap.add_argument("--c5-edge", type=int, default=1024)
+    ap.add_argument("--c5-no-reference", action="store_true")
     args = ap.parse_args()
     if args.ncu_case:
         from fast_gb300 import build
         build.build()
         run_ncu_case(args)
+        return
+    if args.workload != "c2":
+        from fast_gb300 import build
+        build.build()
+        import torch
+        torch.cuda.set_device(0)
+        {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
         return
     ws, rank, local = dist_init()
     if args.impl == "reference":

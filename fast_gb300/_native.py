@@ -30,6 +30,28 @@ class fast_tau_result(C.Structure):
     ]
 
 
+class fast_tau_volume(C.Structure):
+    _fields_ = [("mask", C.c_void_p), ("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64),
+                ("dir", C.c_int32), ("reserved", C.c_int32)]
+
+
+class fast_ctx_config(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("face_mean", C.c_int32), ("tolerance", C.c_double),
+                ("max_iter", C.c_uint64), ("d0", C.c_double), ("d1", C.c_double), ("chunk", C.c_int32),
+                ("max_inflight", C.c_int32), ("hbm_budget", C.c_uint64)]
+
+
+class fast_ctx_completion(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("result", fast_tau_result), ("dir", C.c_int32), ("solver", C.c_int32),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+
+class fast_ctx_stats(C.Structure):
+    _fields_ = [("pending", C.c_uint64), ("inflight", C.c_uint64), ("completed", C.c_uint64),
+                ("admitted", C.c_uint64), ("steps", C.c_uint64), ("bytes_inflight", C.c_uint64),
+                ("hbm_budget", C.c_uint64), ("now", C.c_double)]
+
+
 K_COUNT = 16
 KERNEL_NAMES = ["code", "init", "cg1", "cg2", "bi_restart", "bi1", "bi2", "bi3", "replace", "init64", "tau"]
 FLAG_PROFILE = 1
@@ -57,6 +79,17 @@ SIGNATURES = {
     "fast_tau_last_stats": (C.c_int, [C.POINTER(fast_tau_stats)]),
     "fast_porosity_device_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_uint64),
                                                C.POINTER(C.c_double), C.c_void_p]),
+    "fast_tau_solve_batch": (C.c_int, [C.POINTER(fast_tau_volume), C.c_int32, C.POINTER(fast_tau_params),
+                                       C.POINTER(fast_tau_result)]),
+    "fast_tau_solve_batch_device": (C.c_int, [C.POINTER(fast_tau_volume), C.c_int32, C.POINTER(fast_tau_params),
+                                              C.POINTER(fast_tau_result), C.c_void_p]),
+    "fast_ctx_config_init": (None, [C.POINTER(fast_ctx_config)]),
+    "fast_ctx_create": (C.c_int, [C.POINTER(fast_ctx_config), C.POINTER(C.c_void_p)]),
+    "fast_ctx_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32,
+                                  C.POINTER(C.c_uint64)]),
+    "fast_ctx_poll": (C.c_int, [C.c_void_p, C.POINTER(fast_ctx_completion), C.c_int32, C.POINTER(C.c_int32)]),
+    "fast_ctx_query": (C.c_int, [C.c_void_p, C.POINTER(fast_ctx_stats)]),
+    "fast_ctx_destroy": (C.c_int, [C.c_void_p]),
     "fast_ccl_label": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint8, C.c_void_p,
                                  C.POINTER(C.c_uint32), C.c_void_p, C.c_uint64]),
     "fast_ccl_label_device": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint8, C.c_void_p,

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(ROOT, "include")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfasttau.so")
 
-CUDA_SOURCES = ["kern_f64.cu", "kern_f32.cu", "kern_misc.cu", "tau_host.cu", "noalloc.cu", "ccl.cu"]
+CUDA_SOURCES = ["kern_f64.cu", "kern_f32.cu", "kern_misc.cu", "tau_host.cu", "noalloc.cu", "ccl.cu", "serve.cu"]
 CXX_SOURCES = ["gen.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

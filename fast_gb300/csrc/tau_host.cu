@@ -24,8 +24,7 @@
 #include <vector>
 
 #include "fasttau.h"
-#include "tau_launch.h"
-#include "tau_types.h"
+#include "tau_engine.h"
 
 using namespace ft;
 
@@ -70,35 +69,27 @@ void ft_clear_error() { g_last_error.clear(); }
 // ---------------------------------------------------------------------------
 // Per-thread engine: one non-blocking stream per device, pinned staging.
 // ---------------------------------------------------------------------------
-namespace {
+namespace ft {
 
-struct Engine {
-    int device = -1;
-    cudaStream_t stream = nullptr;
-    Scalars *h_sc = nullptr;   // pinned, 2 * kMaxJobs (double-buffered poll)
-    Job *h_jobs = nullptr;     // pinned staging for job descriptors
-    static constexpr int kMaxJobs = 1024;
-
-    int init(int dev)
-    {
-        device = dev;
-        CU(cudaSetDevice(dev));
-        CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        CU(cudaMallocHost(&h_sc, sizeof(Scalars) * 2 * kMaxJobs));
-        CU(cudaMallocHost(&h_jobs, sizeof(Job) * kMaxJobs));
-        cudaError_t ce = configure_f64();
-        if (ce == cudaSuccess) ce = configure_f32();
-        if (ce == cudaSuccess) ce = configure_misc();
-        if (ce != cudaSuccess) return fail(FAST_CUDA_ERROR, "kernel configuration: %s", cudaGetErrorString(ce));
-        // Keep freed pool memory for reuse by the next solve.
-        cudaMemPool_t pool;
-        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-            uint64_t thr = std::numeric_limits<uint64_t>::max();
-            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-        }
-        return FAST_OK;
+int Engine::init(int dev)
+{
+    device = dev;
+    CU(cudaSetDevice(dev));
+    CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CU(cudaMallocHost(&h_sc, sizeof(Scalars) * 2 * kMaxJobs));
+    CU(cudaMallocHost(&h_jobs, sizeof(Job) * 2 * kMaxJobs));  // jobs + one code job per volume
+    cudaError_t ce = configure_f64();
+    if (ce == cudaSuccess) ce = configure_f32();
+    if (ce == cudaSuccess) ce = configure_misc();
+    if (ce != cudaSuccess) return fail(FAST_CUDA_ERROR, "kernel configuration: %s", cudaGetErrorString(ce));
+    // Keep freed pool memory for reuse by the next solve.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = std::numeric_limits<uint64_t>::max();
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
-};
+    return FAST_OK;
+}
 
 thread_local Engine *t_engines[64] = {};
 
@@ -225,12 +216,6 @@ void fill_tables(Job &J, double d0, double d1, int face_mean)
     J.c_tau[1] = (float)d1;
 }
 
-struct Geometry {
-    int64_t nx, ny, nz, N;
-    int zc, tx, ty, tz;
-    int64_t ntiles;
-};
-
 Geometry make_geometry(int64_t nx, int64_t ny, int64_t nz)
 {
     Geometry g;
@@ -249,8 +234,6 @@ Geometry make_geometry(int64_t nx, int64_t ny, int64_t nz)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-// Row pitch (elements) of every array of a volume: nx rounded up to 16, so a
-// row of any element size starts on a 16-byte boundary (TMA stride rule).
 int64_t row_pitch(int64_t nx) { return (nx + 15) / 16 * 16; }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
@@ -284,18 +267,6 @@ int tensor_map(CUtensorMap *tm, const void *base, int es, int64_t nx, int64_t ny
     if (r != CUDA_SUCCESS) return fail(FAST_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return FAST_OK;
 }
-
-// Device memory of one multi-direction solve, carved from one allocation.
-struct Arena {
-    char *base = nullptr;
-    size_t off = 0, cap = 0;
-    void *take(size_t bytes)
-    {
-        void *p = base + off;
-        off += align_up(bytes, 256);
-        return p;
-    }
-};
 
 // Replays `chunk` iterations from a captured graph until every job has left
 // RUNNING; polls the device scalars one chunk behind so the queue never
@@ -406,29 +377,138 @@ int status_of(int state)
     }
 }
 
-// The whole multi-direction solve on a device-resident mask.
-int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, const fast_tau_params &P,
-                 int ndirs, const int32_t *dirs, fast_tau_result *res, void *conc_out)
+// A volume of a solve (device-resident mask) and a right-hand side of it.
+struct VolSpec {
+    const uint8_t *d_mask;
+    int64_t nx, ny, nz;
+};
+struct JobSpec {
+    int vol;
+    int dir;
+};
+
+size_t code_bytes(int64_t nx, int64_t ny, int64_t nz) { return align_up((size_t)(row_pitch(nx) * ny * nz), 256); }
+
+size_t job_bytes(int64_t nx, int64_t ny, int64_t nz, int prec, int solver)
+{
+    const bool mixed = prec == FAST_PREC_MIXED;
+    const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
+    const size_t nvec = (solver == FAST_SOLVER_CG) ? 4 : 8;
+    const size_t NP = (size_t)(row_pitch(nx) * ny * nz);
+    const Geometry G = make_geometry(nx, ny, nz);
+    return nvec * align_up(NP * vec_t, 256) + (mixed ? 2 * align_up(NP * 8, 256) : 0) +
+           align_up((size_t)G.ntiles * NPART * sizeof(double), 256);
+}
+
+// Device bytes of a solve: one stencil-code array per volume, the state
+// vectors, partial sums and scalars of every right-hand side.
+size_t solve_bytes(const std::vector<VolSpec> &vols, const std::vector<JobSpec> &jobs, int prec, int solver)
+{
+    size_t need = 4096;
+    for (const VolSpec &v : vols) need += code_bytes(v.nx, v.ny, v.nz);
+    for (const JobSpec &j : jobs) need += job_bytes(vols[j.vol].nx, vols[j.vol].ny, vols[j.vol].nz, prec, solver);
+    const size_t nj = jobs.size(), nv = vols.size();
+    need += align_up(sizeof(Scalars) * nj, 256) + align_up(sizeof(uint32_t) * nj, 256) +
+            align_up(sizeof(Job) * (nj + nv), 256);
+    return need;
+}
+
+int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, int dir,
+              const uint8_t *d_code, Scalars *d_sc, uint32_t *d_counter, Arena &A, const fast_tau_params &P)
+{
+    const int prec = P.precision, solver = P.solver;
+    const bool mixed = prec == FAST_PREC_MIXED;
+    const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
+    const Geometry G = make_geometry(nx, ny, nz);
+    const int64_t pitch = row_pitch(nx);
+    const int64_t NP = pitch * ny * nz;
+    const size_t vbytes = align_up((size_t)NP * vec_t, 256);
+    const size_t v64 = align_up((size_t)NP * 8, 256);
+    memset(&J, 0, sizeof(Job));
+    memset(&S, 0, sizeof(Scalars));
+    J.nx = (int32_t)nx; J.ny = (int32_t)ny; J.nz = (int32_t)nz;
+    J.pitch = (int32_t)pitch;
+    J.dir = dir;
+    J.tiles_x = G.tx; J.tiles_y = G.ty; J.tiles_z = G.tz;
+    J.zc = G.zc;
+    J.ntiles = G.ntiles;
+    J.code = d_code;
+    J.mask = d_mask;
+    J.x = A.take(vbytes);
+    J.r[0] = A.take(vbytes);
+    J.p[0] = A.take(vbytes);
+    J.p[1] = A.take(vbytes);
+    if (solver == FAST_SOLVER_BICGSTAB) {
+        J.r[1] = A.take(vbytes);
+        J.r0 = A.take(vbytes);
+        J.v[0] = A.take(vbytes);
+        J.v[1] = A.take(vbytes);
+    }
+    if (mixed) {
+        J.x64[0] = (double *)A.take(v64);
+        J.x64[1] = (double *)A.take(v64);
+    }
+    J.part = (double *)A.take((size_t)G.ntiles * NPART * sizeof(double));
+    if (A.off > A.cap) return fail(FAST_CUDA_ERROR, "internal: device plan overflow");
+    const int es = (int)vec_t;
+    int ts = tensor_map(&J.tm[TM_CODE], J.code, 1, nx, ny, nz, pitch);
+    if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_X], J.x, es, nx, ny, nz, pitch);
+    if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R], J.r[0], es, nx, ny, nz, pitch);
+    if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P], J.p[0], es, nx, ny, nz, pitch);
+    if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P + 1], J.p[1], es, nx, ny, nz, pitch);
+    if (ts == FAST_OK && solver == FAST_SOLVER_BICGSTAB) {
+        ts = tensor_map(&J.tm[TM_R + 1], J.r[1], es, nx, ny, nz, pitch);
+        if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R0], J.r0, es, nx, ny, nz, pitch);
+        if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_V], J.v[0], es, nx, ny, nz, pitch);
+        if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_V + 1], J.v[1], es, nx, ny, nz, pitch);
+    }
+    if (ts == FAST_OK && mixed) {
+        ts = tensor_map(&J.tm[TM_X64], J.x64[0], 8, nx, ny, nz, pitch);
+        if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_X64 + 1], J.x64[1], 8, nx, ny, nz, pitch);
+    }
+    if (ts != FAST_OK) return ts;
+    J.sc = d_sc;
+    J.counter = d_counter;
+    fill_tables(J, P.d0, P.d1, P.face_mean);
+
+    const int64_t maxdim = std::max(nx, std::max(ny, nz));
+    const float h = 1.0f / (float)maxdim;  // cellDim = vec3(1.0f / maxDim) (VolumeMeasures.cpp:68)
+    const double h2 = (double)h * (double)h;
+    // Solver tolerance is T-typed (Solver.h:155-158).
+    S.tol = (prec == FAST_PREC_F32) ? (double)(float)P.tolerance : P.tolerance;
+    S.max_iter = P.max_iter;
+    S.div_thresh = 10e+10 / h2;  // |r|^2 > 1e11 in the reference's h-scaled units
+    S.eps2 = (prec == FAST_PREC_F64) ? (double)DBL_EPSILON * DBL_EPSILON : (double)FLT_EPSILON * (double)FLT_EPSILON;
+    S.state = RUNNING;
+    S.tol_outer = P.tolerance;
+    // MIXED: the first step is a replacement with restart (x64 = x0, e = 0).
+    S.replace = mixed ? 2 : 0;
+    const double delta = env_double("FAST_TAU_REPLACE_DELTA", 0.1);
+    S.delta2 = delta * delta;
+    const double cmin = env_double("FAST_TAU_SHADOW_COS", 1e-4);
+    S.cos2_min = cmin * cmin;
+    S.inner_mode = mixed ? 1 : 0;
+    return FAST_OK;
+}
+
+// Solves every right-hand side of `jobs` (directions of the volumes in
+// `vols`) together: one launch per solver step covers all of them, each
+// block working for one (job, tile); converged right-hand sides drop out of
+// the launches at block entry.  conc_out: only with a single job.
+int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<JobSpec> &jobs,
+               const fast_tau_params &P, fast_tau_result *res, void *conc_out)
 {
     cudaStream_t st = E.stream;
     t_prof.reset((P.flags & FAST_FLAG_PROFILE) != 0);
     const int prec = P.precision, solver = P.solver;
-    const Geometry G = make_geometry(nx, ny, nz);
-    const int64_t N = G.N;
     const bool mixed = prec == FAST_PREC_MIXED;
+    const int nj = (int)jobs.size(), nv = (int)vols.size();
+    if (nj < 1 || nj > Engine::kMaxJobs || nv < 1 || nv > nj)
+        return fail(FAST_BAD_ARG, "1..%d right-hand sides per call", Engine::kMaxJobs);
+    const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
 
     // --- memory plan (the reference's fit check, VolumeMeasures.cpp:104-125)
-    const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
-    const int64_t pitch = row_pitch(nx);
-    const int64_t NP = pitch * ny * nz;  // padded element count of every array
-    const size_t vbytes = align_up((size_t)NP * vec_t, 256);
-    const size_t v64 = align_up((size_t)NP * 8, 256);
-    const size_t nvec = (solver == FAST_SOLVER_CG) ? 4 : 8;
-    const size_t part_bytes = align_up((size_t)G.ntiles * NPART * sizeof(double), 256);
-    size_t need = align_up((size_t)NP, 256)                                 // stencil codes
-                  + (size_t)ndirs * (nvec * vbytes + (mixed ? 2 * v64 : 0) + part_bytes)
-                  + align_up(sizeof(Scalars) * ndirs, 256) + align_up(sizeof(uint32_t) * ndirs, 256)
-                  + align_up(sizeof(Job) * ndirs, 256) + 4096;
+    const size_t need = solve_bytes(vols, jobs, prec, solver);
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
     if (need > free_b) {
@@ -450,107 +530,66 @@ int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64
     Arena A;
     CU(cudaMallocAsync((void **)&A.base, need, st));
     A.cap = need;
-    uint8_t *d_code = (uint8_t *)A.take((size_t)NP);
-    Scalars *d_sc = (Scalars *)A.take(sizeof(Scalars) * ndirs);
-    uint32_t *d_cnt = (uint32_t *)A.take(sizeof(uint32_t) * ndirs);
-    Job *d_jobs = (Job *)A.take(sizeof(Job) * ndirs);
+    Scalars *d_sc = (Scalars *)A.take(sizeof(Scalars) * nj);
+    uint32_t *d_cnt = (uint32_t *)A.take(sizeof(uint32_t) * nj);
+    Job *d_jobs = (Job *)A.take(sizeof(Job) * (nj + nv));  // jobs, then one code job per volume
+    std::vector<uint8_t *> d_code(nv);
+    std::vector<int> first_job(nv, -1);
+    for (int v = 0; v < nv; v++) {
+        const VolSpec &V = vols[v];
+        d_code[v] = (uint8_t *)A.take((size_t)(row_pitch(V.nx) * V.ny * V.nz));
+    }
+    for (int j = 0; j < nj; j++)
+        if (first_job[jobs[j].vol] < 0) first_job[jobs[j].vol] = j;
 
     // --- job descriptors
-    int64_t maxdim = std::max(nx, std::max(ny, nz));
-    const float h = 1.0f / (float)maxdim;  // cellDim = vec3(1.0f / maxDim) (VolumeMeasures.cpp:68)
-    const double h2 = (double)h * (double)h;
     Job *hj = E.h_jobs;
     Scalars *hs = E.h_sc;  // staging (the poll buffers are not in use yet)
-    memset(hj, 0, sizeof(Job) * ndirs);
-    memset(hs, 0, sizeof(Scalars) * ndirs);
-    for (int j = 0; j < ndirs; j++) {
-        Job &J = hj[j];
-        J.nx = (int32_t)nx; J.ny = (int32_t)ny; J.nz = (int32_t)nz;
-        J.pitch = (int32_t)pitch;
-        J.dir = dirs[j];
-        J.tiles_x = G.tx; J.tiles_y = G.ty; J.tiles_z = G.tz;
-        J.zc = G.zc;
-        J.tile_base = (int64_t)j * G.ntiles;
-        J.ntiles = G.ntiles;
-        J.code = d_code;
-        J.mask = d_mask;
-        J.x = A.take(vbytes);
-        J.r[0] = A.take(vbytes);
-        J.p[0] = A.take(vbytes);
-        J.p[1] = A.take(vbytes);
-        if (solver == FAST_SOLVER_BICGSTAB) {
-            J.r[1] = A.take(vbytes);
-            J.r0 = A.take(vbytes);
-            J.v[0] = A.take(vbytes);
-            J.v[1] = A.take(vbytes);
+    int64_t tile_base = 0;
+    for (int j = 0; j < nj; j++) {
+        const VolSpec &V = vols[jobs[j].vol];
+        const int bs = build_job(hj[j], hs[j], V.d_mask, V.nx, V.ny, V.nz, jobs[j].dir, d_code[jobs[j].vol], d_sc + j,
+                                 d_cnt + j, A, P);
+        if (bs != FAST_OK) {
+            cudaFreeAsync(A.base, st);
+            cudaStreamSynchronize(st);
+            return bs;
         }
-        if (mixed) {
-            J.x64[0] = (double *)A.take(v64);
-            J.x64[1] = (double *)A.take(v64);
-        }
-        J.part = (double *)A.take(part_bytes);
-        {
-            const int es = (int)vec_t;
-            int ts = tensor_map(&J.tm[TM_CODE], d_code, 1, nx, ny, nz, pitch);
-            if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_X], J.x, es, nx, ny, nz, pitch);
-            if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R], J.r[0], es, nx, ny, nz, pitch);
-            if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P], J.p[0], es, nx, ny, nz, pitch);
-            if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P + 1], J.p[1], es, nx, ny, nz, pitch);
-            if (ts == FAST_OK && solver == FAST_SOLVER_BICGSTAB) {
-                ts = tensor_map(&J.tm[TM_R + 1], J.r[1], es, nx, ny, nz, pitch);
-                if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R0], J.r0, es, nx, ny, nz, pitch);
-                if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_V], J.v[0], es, nx, ny, nz, pitch);
-                if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_V + 1], J.v[1], es, nx, ny, nz, pitch);
-            }
-            if (ts == FAST_OK && mixed) {
-                ts = tensor_map(&J.tm[TM_X64], J.x64[0], 8, nx, ny, nz, pitch);
-                if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_X64 + 1], J.x64[1], 8, nx, ny, nz, pitch);
-            }
-            if (ts != FAST_OK) {
-                cudaFreeAsync(A.base, st);
-                cudaStreamSynchronize(st);
-                return ts;
-            }
-        }
-        J.sc = d_sc + j;
-        J.counter = d_cnt + j;
-        fill_tables(J, P.d0, P.d1, P.face_mean);
-
-        Scalars &S = hs[j];
-        // Solver tolerance is T-typed (Solver.h:155-158).
-        S.tol = (prec == FAST_PREC_F32) ? (double)(float)P.tolerance : P.tolerance;
-        S.max_iter = P.max_iter;
-        S.div_thresh = 10e+10 / h2;  // |r|^2 > 1e11 in the reference's h-scaled units
-        S.eps2 = (prec == FAST_PREC_F64) ? (double)DBL_EPSILON * DBL_EPSILON
-                                         : (double)FLT_EPSILON * (double)FLT_EPSILON;
-        S.state = RUNNING;
-        S.tol_outer = P.tolerance;
-        // MIXED: the first step is a replacement with restart (x64 = x0, e = 0).
-        S.replace = mixed ? 2 : 0;
-        const double delta = env_double("FAST_TAU_REPLACE_DELTA", 0.1);
-        S.delta2 = delta * delta;
-        const double cmin = env_double("FAST_TAU_SHADOW_COS", 1e-4);
-        S.cos2_min = cmin * cmin;
-        S.inner_mode = mixed ? 1 : 0;
+        hj[j].tile_base = tile_base;
+        tile_base += hj[j].ntiles;
     }
-    CU(cudaMemcpyAsync(d_jobs, hj, sizeof(Job) * ndirs, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(d_sc, hs, sizeof(Scalars) * ndirs, cudaMemcpyHostToDevice, st));
-    CU(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t) * ndirs, st));
+    // One stencil-code job per volume (a copy of its first right-hand side
+    // with its own tile numbering); the pore count lands in that job's scalars.
+    int64_t code_base = 0;
+    for (int v = 0; v < nv; v++) {
+        Job &C = hj[nj + v];
+        C = hj[first_job[v]];
+        C.tile_base = code_base;
+        code_base += C.ntiles;
+    }
+    if (tile_base > (int64_t)INT32_MAX || code_base > (int64_t)INT32_MAX) {
+        cudaFreeAsync(A.base, st);
+        cudaStreamSynchronize(st);
+        return fail(FAST_BAD_ARG, "too many tiles in one launch (%lld)", (long long)tile_base);
+    }
+    CU(cudaMemcpyAsync(d_jobs, hj, sizeof(Job) * (nj + nv), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_sc, hs, sizeof(Scalars) * nj, cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t) * nj, st));
     // The staging buffers are reused below: wait for the copies to land.
     CU(cudaStreamSynchronize(st));
 
-    Launch L{d_jobs, ndirs, 0, (int64_t)ndirs * G.ntiles};
-    Launch L1{d_jobs, 1, 0, G.ntiles};  // the volume itself (codes + porosity)
+    Launch L{d_jobs, nj, 0, tile_base};
+    Launch LC{d_jobs + nj, nv, 0, code_base};
 
     int status = FAST_OK;
-    launch_counted(FAST_K_CODE, st, [&] { launch_code(L1, st); });
+    launch_counted(FAST_K_CODE, st, [&] { launch_code(LC, st); });
     if (!mixed) {
         void (*fn)(Step, const Launch &, cudaStream_t) = (prec == FAST_PREC_F64) ? dispatch_f64 : dispatch_f32;
         launch_counted(FAST_K_INIT, st, [&] { fn(solver == FAST_SOLVER_CG ? Step::INIT_CG : Step::INIT_BI, L, st); });
         std::vector<Step> steps;
         if (solver == FAST_SOLVER_CG) steps = {Step::CG1, Step::CG2};
         else steps = {Step::BI_RESTART, Step::BI1, Step::BI2, Step::BI3};
-        status = iterate(E, L, ndirs, d_sc, steps, fn, P.max_iter);
+        status = iterate(E, L, nj, d_sc, steps, fn, P.max_iter);
     } else {
         // FP32 iterations with in-graph FP64 residual replacement: the
         // replacement slot leads every iteration and is a no-op launch unless
@@ -559,12 +598,12 @@ int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64
         std::vector<Step> steps;
         if (solver == FAST_SOLVER_CG) steps = {Step::REPLACE_CG, Step::CG1, Step::CG2};
         else steps = {Step::REPLACE_BI, Step::BI1, Step::BI2, Step::BI3};
-        status = iterate(E, L, ndirs, d_sc, steps, dispatch_mixed, P.max_iter);
+        status = iterate(E, L, nj, d_sc, steps, dispatch_mixed, P.max_iter);
     }
     if (status == FAST_OK)
         launch_counted(FAST_K_TAU, st, [&] { launch_tau(mixed ? 2 : (prec == FAST_PREC_F32 ? 1 : 0), L, st); });
-    CU(cudaMemcpyAsync(hs, d_sc, sizeof(Scalars) * ndirs, cudaMemcpyDeviceToHost, st));
-    if (conc_out && ndirs == 1) {
+    CU(cudaMemcpyAsync(hs, d_sc, sizeof(Scalars) * nj, cudaMemcpyDeviceToHost, st));
+    if (conc_out && nj == 1) {
         const void *src = hj[0].x;
         size_t es = vec_t;
         CU(cudaStreamSynchronize(st));
@@ -573,20 +612,23 @@ int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64
             es = 8;
         }
         // de-pad the rows: host layout is x-fastest with pitch nx
-        CU(cudaMemcpy2DAsync(conc_out, (size_t)nx * es, src, (size_t)pitch * es, (size_t)nx * es, (size_t)(ny * nz),
-                             cudaMemcpyDeviceToHost, st));
+        const int64_t nx = vols[0].nx;
+        CU(cudaMemcpy2DAsync(conc_out, (size_t)nx * es, src, (size_t)hj[0].pitch * es, (size_t)nx * es,
+                             (size_t)(vols[0].ny * vols[0].nz), cudaMemcpyDeviceToHost, st));
     }
     cudaError_t ferr = cudaFreeAsync(A.base, st);
     CU(cudaStreamSynchronize(st));
     if (ferr != cudaSuccess) return fail(FAST_CUDA_ERROR, "cudaFreeAsync: %s", cudaGetErrorString(ferr));
     if (status != FAST_OK) return status;
 
-    // --- results (the stencil-code pass counted the pores into job 0)
-    const uint64_t pores = hs[0].pores;
+    // --- results (the stencil-code pass counted each volume's pores into its
+    // first right-hand side)
     int first_bad = FAST_OK;
-    for (int j = 0; j < ndirs; j++) {
+    for (int j = 0; j < nj; j++) {
         Scalars &S = hs[j];
-        S.pores = pores;
+        const VolSpec &V = vols[jobs[j].vol];
+        const uint64_t pores = hs[first_job[jobs[j].vol]].pores;
+        const int64_t N = V.nx * V.ny * V.nz;
         fast_tau_result &R = res[j];
         memset(&R, 0, sizeof(R));
         R.status = status_of(S.state);
@@ -595,45 +637,74 @@ int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64
         if (mixed) R.rel_residual = S.b64_sq > 0 ? std::sqrt(S.r64_sq / S.b64_sq) : 0.0;
         else R.rel_residual = S.rhs_sq > 0 ? std::sqrt(S.rsq / S.rhs_sq) : 0.0;
         // Porosity: precomputed by the caller, or getPorosity<T> (VolumeMeasures.cpp:179-181).
-        const int k = dirs[j] >> 1;
-        const int64_t dimk = k == 0 ? nx : (k == 1 ? ny : nz);
+        const int k = jobs[j].dir >> 1;
+        const int64_t dimk = k == 0 ? V.nx : (k == 1 ? V.ny : V.nz);
         const int64_t nplane = N / dimk;
         if (prec == FAST_PREC_F32) {
-            const float phi = P.porosity >= 0 ? (float)P.porosity : (float)S.pores / (float)N;
+            const float phi = P.porosity >= 0 ? (float)P.porosity : (float)pores / (float)N;
             R.porosity = phi;
             // tau = porosity / (dc * n_k), dc = sum over planes of (plane sum / n) / n_k
             const float S32 = (float)S.flux_sum;
             const float dc = (S32 / (float)nplane) / (float)dimk;
             R.tau = (R.status == FAST_OK) ? (double)(phi / (dc * (float)dimk)) : 0.0;
         } else {
-            const double phi = P.porosity >= 0 ? P.porosity : (double)S.pores / (double)N;
+            const double phi = P.porosity >= 0 ? P.porosity : (double)pores / (double)N;
             R.porosity = phi;
             const double dc = (S.flux_sum / (double)nplane) / (double)dimk;
             R.tau = (R.status == FAST_OK) ? phi / (dc * (double)dimk) : 0.0;
         }
         if (R.status != FAST_OK && first_bad == FAST_OK) {
             first_bad = R.status;
-            fail(R.status, "direction %d: solver %s after %llu iterations (|r|/|b| = %.3e)", dirs[j],
-                 R.status == FAST_DIVERGED ? "diverged" : "did not converge",
+            fail(R.status, "right-hand side %d (direction %d): solver %s after %llu iterations (|r|/|b| = %.3e)", j,
+                 jobs[j].dir, R.status == FAST_DIVERGED ? "diverged" : "did not converge",
                  (unsigned long long)R.iterations, R.rel_residual);
         }
         if (P.verbose)
-            fprintf(stderr, "fasttau: dir %d tau %.10g iters %llu outer %u relres %.3e status %d\n", dirs[j], R.tau,
-                    (unsigned long long)R.iterations, R.outer_steps, R.rel_residual, R.status);
+            fprintf(stderr, "fasttau: rhs %d dir %d tau %.10g iters %llu outer %u relres %.3e status %d\n", j,
+                    jobs[j].dir, R.tau, (unsigned long long)R.iterations, R.outer_steps, R.rel_residual, R.status);
     }
     return first_bad;
+}
+
+// The multi-direction solve of one device-resident volume.
+int solve_device(Engine &E, const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, const fast_tau_params &P,
+                 int ndirs, const int32_t *dirs, fast_tau_result *res, void *conc_out)
+{
+    std::vector<VolSpec> vols{{d_mask, nx, ny, nz}};
+    std::vector<JobSpec> jobs;
+    for (int j = 0; j < ndirs; j++) jobs.push_back({0, dirs[j]});
+    return solve_jobs(E, vols, jobs, P, res, conc_out);
+}
+
+int check_params(const fast_tau_params *p);
+
+int check_volume(const void *mask, int64_t nx, int64_t ny, int64_t nz)
+{
+    if (!mask) return fail(FAST_NO_HOST_DATA, "mask must be allocated (VolumeMeasures.cpp:55)");
+    if (nx <= 0 || ny <= 0 || nz <= 0) return fail(FAST_BAD_ARG, "dimensions must be positive");
+    if (nx > INT32_MAX / 2 || ny > INT32_MAX / 2 || nz > INT32_MAX / 2)
+        return fail(FAST_BAD_ARG, "dimension too large");
+    return FAST_OK;
 }
 
 int check_args(const void *mask, int64_t nx, int64_t ny, int64_t nz, const fast_tau_params *p, int ndirs,
                const int32_t *dirs)
 {
-    if (!mask) return fail(FAST_NO_HOST_DATA, "mask must be allocated (VolumeMeasures.cpp:55)");
+    int s = check_volume(mask, nx, ny, nz);
+    if (s != FAST_OK) return s;
     if (!p) return fail(FAST_BAD_ARG, "params is NULL");
-    if (nx <= 0 || ny <= 0 || nz <= 0) return fail(FAST_BAD_ARG, "dimensions must be positive");
-    if (nx > INT32_MAX / 2 || ny > INT32_MAX / 2 || nz > INT32_MAX / 2)
-        return fail(FAST_BAD_ARG, "dimension too large");
     const Geometry G = make_geometry(nx, ny, nz);
     if (G.ntiles * (int64_t)std::max(ndirs, 1) > (int64_t)INT32_MAX) return fail(FAST_BAD_ARG, "volume too large");
+    s = check_params(p);
+    if (s != FAST_OK) return s;
+    if (ndirs < 1 || ndirs > 6 || !dirs) return fail(FAST_BAD_ARG, "need 1..6 directions");
+    for (int j = 0; j < ndirs; j++)
+        if (dirs[j] < 0 || dirs[j] > 5) return fail(FAST_BAD_ARG, "bad direction %d", dirs[j]);
+    return FAST_OK;
+}
+
+int check_params(const fast_tau_params *p)
+{
     if (p->solver != FAST_SOLVER_BICGSTAB && p->solver != FAST_SOLVER_CG)
         return fail(FAST_BAD_ARG, "Unknown solver %d", p->solver);
     if (p->precision < FAST_PREC_F64 || p->precision > FAST_PREC_MIXED)
@@ -642,10 +713,20 @@ int check_args(const void *mask, int64_t nx, int64_t ny, int64_t nz, const fast_
         return fail(FAST_BAD_ARG, "unknown face mean %d", p->face_mean);
     if (!(p->tolerance >= 0.0)) return fail(FAST_BAD_ARG, "tolerance must be >= 0");
     if (!(p->d0 > 0.0) || !(p->d1 > 0.0)) return fail(FAST_BAD_ARG, "diffusivities must be positive");
-    if (ndirs < 1 || ndirs > 6 || !dirs) return fail(FAST_BAD_ARG, "need 1..6 directions");
-    for (int j = 0; j < ndirs; j++)
-        if (dirs[j] < 0 || dirs[j] > 5) return fail(FAST_BAD_ARG, "bad direction %d", dirs[j]);
     return FAST_OK;
+}
+
+int check_batch(const fast_tau_volume *vols, int32_t nvols, const fast_tau_params *p, const fast_tau_result *res)
+{
+    if (!vols || !res) return fail(FAST_BAD_ARG, "volumes or results is NULL");
+    if (!p) return fail(FAST_BAD_ARG, "params is NULL");
+    if (nvols < 1 || nvols > 1024) return fail(FAST_BAD_ARG, "need 1..1024 volumes, got %d", nvols);
+    for (int32_t v = 0; v < nvols; v++) {
+        const int s = check_volume(vols[v].mask, vols[v].nx, vols[v].ny, vols[v].nz);
+        if (s != FAST_OK) return fail(s, "volume %d: %s", v, g_last_error.c_str());
+        if (vols[v].dir < 0 || vols[v].dir > 5) return fail(FAST_BAD_ARG, "volume %d: bad direction %d", v, vols[v].dir);
+    }
+    return check_params(p);
 }
 
 }  // namespace
@@ -696,6 +777,59 @@ FAST_API int fast_tau_solve_dirs_device(const uint8_t *d_mask, int64_t nx, int64
     if (stream) E->stream = (cudaStream_t)stream;
     st = solve_device(*E, d_mask, nx, ny, nz, *p, ndirs, dirs, results, nullptr);
     E->stream = saved;
+    return st;
+}
+
+FAST_API int fast_tau_solve_batch_device(const fast_tau_volume *vols, int32_t nvols, const fast_tau_params *p,
+                                         fast_tau_result *results, void *stream)
+{
+    g_last_error.clear();
+    int st = check_batch(vols, nvols, p, results);
+    if (st != FAST_OK) return st;
+    Engine *E = nullptr;
+    st = get_engine(&E);
+    if (st != FAST_OK) return st;
+    std::vector<VolSpec> vs;
+    std::vector<JobSpec> js;
+    for (int32_t v = 0; v < nvols; v++) {
+        vs.push_back({vols[v].mask, vols[v].nx, vols[v].ny, vols[v].nz});
+        js.push_back({(int)v, vols[v].dir});
+    }
+    cudaStream_t saved = E->stream;
+    if (stream) E->stream = (cudaStream_t)stream;
+    st = solve_jobs(*E, vs, js, *p, results, nullptr);
+    E->stream = saved;
+    return st;
+}
+
+FAST_API int fast_tau_solve_batch(const fast_tau_volume *vols, int32_t nvols, const fast_tau_params *p,
+                                  fast_tau_result *results)
+{
+    g_last_error.clear();
+    int st = check_batch(vols, nvols, p, results);
+    if (st != FAST_OK) return st;
+    Engine *E = nullptr;
+    st = get_engine(&E);
+    if (st != FAST_OK) return st;
+    size_t total = 0;
+    for (int32_t v = 0; v < nvols; v++) total += align_up((size_t)(vols[v].nx * vols[v].ny * vols[v].nz), 256);
+    uint8_t *d_all = nullptr;
+    CU(cudaMallocAsync((void **)&d_all, total, E->stream));
+    std::vector<VolSpec> vs;
+    std::vector<JobSpec> js;
+    size_t off = 0;
+    cudaError_t e = cudaSuccess;
+    for (int32_t v = 0; v < nvols && e == cudaSuccess; v++) {
+        const size_t n = (size_t)(vols[v].nx * vols[v].ny * vols[v].nz);
+        e = cudaMemcpyAsync(d_all + off, vols[v].mask, n, cudaMemcpyHostToDevice, E->stream);
+        vs.push_back({d_all + off, vols[v].nx, vols[v].ny, vols[v].nz});
+        js.push_back({(int)v, vols[v].dir});
+        off += align_up(n, 256);
+    }
+    if (e != cudaSuccess) st = fail(FAST_CUDA_ERROR, "mask upload: %s", cudaGetErrorString(e));
+    else st = solve_jobs(*E, vs, js, *p, results, nullptr);
+    cudaFreeAsync(d_all, E->stream);
+    cudaStreamSynchronize(E->stream);
     return st;
 }
 

@@ -273,3 +273,57 @@ def solve_directions_device(dev_ptr: int, shape, dirs: Sequence[Dir], params: To
         raise RuntimeError(f"fast_tau_solve_dirs_device: {msg}")
     return [TauResult(r.tau, r.porosity, r.rel_residual, int(r.iterations), int(r.outer_steps), Status(r.status),
                       Dir(d), msg) for r, d in zip(res, dirs)]
+
+
+def _batch_results(res, vols_dirs, msg):
+    return [TauResult(r.tau, r.porosity, r.rel_residual, int(r.iterations), int(r.outer_steps), Status(r.status),
+                      Dir(d), msg) for r, d in zip(res, vols_dirs)]
+
+
+def solve_batch(volumes: Sequence, params: TortuosityParams,
+                solver_type: DiffusionSolverType = DSOLVER_BICGSTAB) -> List[TauResult]:
+    """Many volumes in one call (fast_tau_solve_batch): ``volumes`` is a
+    sequence of (mask, dir) pairs, masks 3-D uint8 [z, y, x] of any sizes.
+    Every right-hand side advances in the same launches and retires as soon
+    as it converges; each result equals solving that volume alone."""
+    masks, dirs = [], []
+    for mask, d in volumes:
+        m = _as_mask(mask)
+        if m is None:
+            raise TypeError("every mask must be a 3-D uint8 array [z, y, x]")
+        masks.append(m)
+        dirs.append(Dir(d))
+    n = len(masks)
+    arr = (_native.fast_tau_volume * n)()
+    for k, (m, d) in enumerate(zip(masks, dirs)):
+        nz, ny, nx = m.shape
+        arr[k].mask = m.ctypes.data
+        arr[k].nx, arr[k].ny, arr[k].nz, arr[k].dir = nx, ny, nz, int(d)
+    p = params.to_c(solver_type)
+    res = (_native.fast_tau_result * n)()
+    st = _native.lib().fast_tau_solve_batch(arr, n, C.byref(p), res)
+    msg = _native.last_error() if st != 0 else ""
+    if st not in (0, Status.NO_CONVERGENCE, Status.DIVERGED):
+        raise RuntimeError(f"fast_tau_solve_batch: {msg}")
+    return _batch_results(res, dirs, msg)
+
+
+def solve_batch_device(volumes: Sequence, params: TortuosityParams,
+                       solver_type: DiffusionSolverType = DSOLVER_BICGSTAB, stream: int = 0) -> List[TauResult]:
+    """As solve_batch on device-resident masks: ``volumes`` is a sequence of
+    (device pointer, (nz, ny, nx), dir)."""
+    n = len(volumes)
+    arr = (_native.fast_tau_volume * n)()
+    dirs = []
+    for k, (ptr, shape, d) in enumerate(volumes):
+        nz, ny, nx = shape
+        arr[k].mask = int(ptr)
+        arr[k].nx, arr[k].ny, arr[k].nz, arr[k].dir = nx, ny, nz, int(d)
+        dirs.append(Dir(d))
+    p = params.to_c(solver_type)
+    res = (_native.fast_tau_result * n)()
+    st = _native.lib().fast_tau_solve_batch_device(arr, n, C.byref(p), res, C.c_void_p(stream) if stream else None)
+    msg = _native.last_error() if st != 0 else ""
+    if st not in (0, Status.NO_CONVERGENCE, Status.DIVERGED):
+        raise RuntimeError(f"fast_tau_solve_batch_device: {msg}")
+    return _batch_results(res, dirs, msg)

@@ -134,6 +134,74 @@ FAST_API int fast_tau_solve_dirs_device(const uint8_t *d_mask, int64_t nx, int64
                                         const int32_t *dirs, fast_tau_result *results,
                                         void *stream);
 
+/* One volume of a batch: a uint8 mask (HOST for fast_tau_solve_batch,
+ * DEVICE for fast_tau_solve_batch_device), its dimensions and the direction
+ * to solve. */
+typedef struct fast_tau_volume {
+    const uint8_t *mask;
+    int64_t nx, ny, nz;
+    int32_t dir;            /* fast_dir */
+    int32_t reserved;
+} fast_tau_volume;
+
+/* Many volumes of different sizes in one call (no counterpart in the
+ * reference, which solves one volume per getTortuosity call): all right-hand
+ * sides advance together, one launch per solver step covering every
+ * (volume, tile) pair, and each is retired as soon as it converges.  Results
+ * are identical to solving each volume alone (the reductions of a right-hand
+ * side never mix with another's).  1..1024 volumes; p->dir is ignored.
+ * Returns the first non-OK status. */
+FAST_API int fast_tau_solve_batch(const fast_tau_volume *vols, int32_t nvols, const fast_tau_params *p,
+                                  fast_tau_result *results);
+FAST_API int fast_tau_solve_batch_device(const fast_tau_volume *vols, int32_t nvols, const fast_tau_params *p,
+                                         fast_tau_result *results, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Serving context: continuous batching of requests on one GPU (no          */
+/* counterpart in the reference, which solves one volume per run).  A       */
+/* context queues submitted requests; every fast_ctx_poll runs one          */
+/* scheduling step: it retires the solves that finished, admits queued      */
+/* requests (oldest first) while a slot is free and their device footprint  */
+/* fits hbm_budget, and advances every in-flight solve by `chunk`           */
+/* iterations in shared launches (one CUDA graph per solver).  A request's  */
+/* result is identical to solving it alone.  A context is used by one host  */
+/* thread at a time.                                                        */
+/* ------------------------------------------------------------------------ */
+typedef struct fast_ctx_config {
+    int32_t precision;      /* fast_precision; default MIXED */
+    int32_t face_mean;      /* fast_face_mean */
+    double tolerance;       /* default 1e-6 */
+    uint64_t max_iter;      /* default 10000 */
+    double d0, d1;          /* default (double)1.0f, (double)0.001f */
+    int32_t chunk;          /* iterations per scheduling step, default 16 */
+    int32_t max_inflight;   /* solves on the GPU at once, 1..1024, default 256 */
+    uint64_t hbm_budget;    /* device bytes for in-flight solves; 0 = 80 % of free memory */
+} fast_ctx_config;
+
+typedef struct fast_ctx_completion {
+    uint64_t ticket;        /* from fast_ctx_submit */
+    fast_tau_result result;
+    int32_t dir, solver;
+    double t_submit, t_admit, t_done;  /* seconds on the context's clock */
+} fast_ctx_completion;
+
+typedef struct fast_ctx_stats {
+    uint64_t pending, inflight, completed, admitted, steps;
+    uint64_t bytes_inflight, hbm_budget;
+    double now;             /* the context's clock, seconds since creation */
+} fast_ctx_stats;
+
+FAST_API void fast_ctx_config_init(fast_ctx_config *cfg);
+FAST_API int fast_ctx_create(const fast_ctx_config *cfg, void **ctx);
+/* Queues a request; the HOST mask is copied, so the caller may free it. */
+FAST_API int fast_ctx_submit(void *ctx, const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, int32_t dir,
+                             int32_t solver, uint64_t *ticket);
+/* One scheduling step; up to `cap` finished requests are written to out and
+ * counted in *n_done (the others are returned by later polls). */
+FAST_API int fast_ctx_poll(void *ctx, fast_ctx_completion *out, int32_t cap, int32_t *n_done);
+FAST_API int fast_ctx_query(void *ctx, fast_ctx_stats *out);
+FAST_API int fast_ctx_destroy(void *ctx);
+
 /* getPorosity<T> (VolumeMeasures.h:60-61 via Volume::sumZeroElems,
  * fastlib/src/volume/Volume.cpp:261-272): fraction of zero voxels, counted on
  * the GPU.  pore_count is nullable. */

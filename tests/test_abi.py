@@ -104,3 +104,42 @@ def test_ccl_argument_errors_without_gpu(native):
     assert native.fast_ccl_label(mp, 4, 4, 4, 255, None, None, None, 0) == 8
     assert native.fast_ccl_label_device(None, 4, 4, 4, 255, None, C.byref(n), None, 0, None) == 8
     assert native.fast_ccl_boundary_device(None, 4, 4, 4, 3, None, None) == 8
+
+
+def test_batch_argument_errors_without_gpu(native):
+    from fast_gb300 import _native
+    p = _native.fast_tau_params()
+    native.fast_tau_params_init(C.byref(p))
+    res = (_native.fast_tau_result * 2)()
+    vols = (_native.fast_tau_volume * 2)()
+    m = np.zeros((4, 4, 4), np.uint8)
+    for v in vols:
+        v.mask = m.ctypes.data
+        v.nx = v.ny = v.nz = 4
+        v.dir = 0
+    assert native.fast_tau_solve_batch(None, 2, C.byref(p), res) == 8
+    assert native.fast_tau_solve_batch(vols, 0, C.byref(p), res) == 8
+    assert native.fast_tau_solve_batch(vols, 2000, C.byref(p), res) == 8
+    vols[1].dir = 7
+    assert native.fast_tau_solve_batch(vols, 2, C.byref(p), res) == 8
+    assert b"volume 1" in native.fast_last_error()
+    vols[1].dir = 0
+    vols[1].mask = None
+    assert native.fast_tau_solve_batch(vols, 2, C.byref(p), res) == 2
+
+
+def test_ctx_argument_errors_without_gpu(native):
+    from fast_gb300 import _native
+    cfg = _native.fast_ctx_config()
+    native.fast_ctx_config_init(C.byref(cfg))
+    assert cfg.precision == 2 and cfg.chunk == 16 and cfg.max_inflight == 256 and cfg.tolerance == 1e-6
+    h = C.c_void_p()
+    assert native.fast_ctx_create(None, C.byref(h)) == 8
+    cfg.chunk = 0
+    assert native.fast_ctx_create(C.byref(cfg), C.byref(h)) == 8
+    cfg.chunk = 16
+    cfg.max_inflight = 5000
+    assert native.fast_ctx_create(C.byref(cfg), C.byref(h)) == 8
+    t = C.c_uint64(0)
+    m = np.zeros((4, 4, 4), np.uint8)
+    assert native.fast_ctx_submit(None, m.ctypes.data_as(C.c_void_p), 4, 4, 4, 0, 0, C.byref(t)) == 8
