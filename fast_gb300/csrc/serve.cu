@@ -14,6 +14,12 @@
 //      and re-capture its chunk graph (`chunk` iterations of the group's
 //      kernels over all of its solves);
 //   5. launch one chunk per group and copy the slot array back behind it.
+// Two chunks are kept in flight: a poll first queues the next chunk of the
+// current solves, then reads the snapshot of the older one, so the GPU keeps
+// iterating while the host retires and admits.  Chunks carry sequence
+// numbers; a snapshot speaks only for solves admitted before its chunk.  All
+// work is on one stream, so a slot or job table reused for a new solve is
+// rewritten only after every queued chunk that names its previous owner.
 // A request's arithmetic is exactly that of a solve of it alone: its kernels
 // see only its own scalars and partial sums, whatever else shares the
 // launches.  There is no counterpart in the reference (fast tau solves one
@@ -57,6 +63,7 @@ struct Active {
     size_t bytes;
     Job job;          // descriptor (tile_base set per launch)
     double t_admit;
+    uint64_t first_seq;  // the first chunk that advances this solve
 };
 
 struct Group {
@@ -74,7 +81,7 @@ struct Ctx {
     int kMax = 0;
     Scalars *d_slots = nullptr;
     uint32_t *d_cnt = nullptr;
-    Scalars *h_snap = nullptr;      // pinned copy of the slot array
+    Scalars *h_snap[2] = {};        // pinned copies of the slot array, one per chunk in flight
     Scalars *h_init = nullptr;      // pinned staging of new solves' scalars
     Job *h_stage = nullptr;         // pinned staging of job tables (5 regions of kMax)
     Job *d_tmp[3] = {};             // device job tables for retire / code / init launches
@@ -83,8 +90,12 @@ struct Ctx {
     std::vector<Active> active;
     Group groups[2];
     bool dirty = true;
-    bool chunk_in_flight = false;
-    cudaEvent_t ev = nullptr;
+    // Up to two chunks in flight: the GPU runs the next one while the host
+    // retires and admits from the snapshot of the previous one.
+    int inflight = 0, head = 0;
+    cudaEvent_t ev[2] = {};
+    uint64_t snap_seq[2] = {};
+    uint64_t next_seq = 0;
     uint64_t next_ticket = 1;
     size_t bytes_inflight = 0;
     uint64_t completed = 0, admitted = 0, steps = 0;
@@ -125,18 +136,20 @@ int upload_jobs(Ctx &C, Job *stage, const std::vector<const Job *> &src, Job *d_
     return FAST_OK;
 }
 
-int retire(Ctx &C, fast_ctx_completion *out, int32_t cap, int32_t &n_out)
+// Retires the solves that the snapshot of chunk `seq` (buffer `snap`) shows
+// finished; solves admitted after that chunk was launched are not in it.
+int retire(Ctx &C, Scalars *snap, uint64_t seq, fast_ctx_completion *out, int32_t cap, int32_t &n_out)
 {
     std::vector<int> done;
     for (int a = 0; a < (int)C.active.size(); a++)
-        if (C.h_snap[C.active[a].slot].state != RUNNING) done.push_back(a);
+        if (C.active[a].first_seq <= seq && snap[C.active[a].slot].state != RUNNING) done.push_back(a);
     if (done.empty()) return FAST_OK;
     // Results go out in the poll that retires them: only as many as fit.
     if ((int32_t)done.size() > cap - n_out) done.resize((size_t)std::max(0, cap - n_out));
     if (done.empty()) return FAST_OK;
     std::vector<const Job *> jobs;
     for (int a : done)
-        if (C.h_snap[C.active[a].slot].state == CONVERGED) jobs.push_back(&C.active[a].job);
+        if (snap[C.active[a].slot].state == CONVERGED) jobs.push_back(&C.active[a].job);
     if (!jobs.empty()) {
         int64_t nb = 0;
         int s = upload_jobs(C, C.h_stage, jobs, C.d_tmp[0], nb);
@@ -148,13 +161,13 @@ int retire(Ctx &C, fast_ctx_completion *out, int32_t cap, int32_t &n_out)
     }
     // Every retiring solve's final scalars (flux sums included).
     for (int a : done)
-        SV(cudaMemcpyAsync(C.h_snap + C.active[a].slot, C.d_slots + C.active[a].slot, sizeof(Scalars),
+        SV(cudaMemcpyAsync(snap + C.active[a].slot, C.d_slots + C.active[a].slot, sizeof(Scalars),
                            cudaMemcpyDeviceToHost, C.st));
     SV(cudaStreamSynchronize(C.st));
     const double t = C.now();
     for (int a : done) {
         Active &A = C.active[a];
-        const Scalars &S = C.h_snap[A.slot];
+        const Scalars &S = snap[A.slot];
         fast_ctx_completion &R = out[n_out++];
         memset(&R, 0, sizeof(R));
         R.ticket = A.req.ticket;
@@ -236,6 +249,7 @@ int admit(Ctx &C)
         A.req.mask.clear();
         A.req.mask.shrink_to_fit();
         A.t_admit = C.now();
+        A.first_seq = C.next_seq;
         C.bytes_inflight += bytes;
         C.admitted++;
         C.active.push_back(std::move(A));
@@ -306,13 +320,36 @@ int rebuild(Ctx &C)
     return FAST_OK;
 }
 
+int launch_chunk(Ctx &C)
+{
+    const int b = (C.head + C.inflight) & 1;
+    for (int g = 0; g < 2; g++)
+        if (C.groups[g].exec) SV(cudaGraphLaunch(C.groups[g].exec, C.st));
+    int hi = 0;
+    for (const Active &A : C.active) hi = std::max(hi, A.slot + 1);
+    SV(cudaMemcpyAsync(C.h_snap[b], C.d_slots, sizeof(Scalars) * hi, cudaMemcpyDeviceToHost, C.st));
+    SV(cudaEventRecord(C.ev[b], C.st));
+    C.snap_seq[b] = C.next_seq++;
+    C.inflight++;
+    C.steps++;
+    return FAST_OK;
+}
+
 int step(Ctx &C, fast_ctx_completion *out, int32_t cap, int32_t *n_out)
 {
     *n_out = 0;
-    if (C.chunk_in_flight) {
-        SV(cudaEventSynchronize(C.ev));
-        C.chunk_in_flight = false;
-        int s = retire(C, out, cap, *n_out);
+    // Keep the GPU busy: queue the next chunk of the current set of solves
+    // before waiting for the previous one.
+    if (C.inflight == 1 && !C.dirty && !C.active.empty()) {
+        int s = launch_chunk(C);
+        if (s != FAST_OK) return s;
+    }
+    if (C.inflight > 0) {
+        const int b = C.head;
+        SV(cudaEventSynchronize(C.ev[b]));
+        C.head ^= 1;
+        C.inflight--;
+        int s = retire(C, C.h_snap[b], C.snap_seq[b], out, cap, *n_out);
         if (s != FAST_OK) return s;
     }
     int s = admit(C);
@@ -322,14 +359,10 @@ int step(Ctx &C, fast_ctx_completion *out, int32_t cap, int32_t *n_out)
         s = rebuild(C);
         if (s != FAST_OK) return s;
     }
-    for (int g = 0; g < 2; g++)
-        if (C.groups[g].exec) SV(cudaGraphLaunch(C.groups[g].exec, C.st));
-    int hi = 0;
-    for (const Active &A : C.active) hi = std::max(hi, A.slot + 1);
-    SV(cudaMemcpyAsync(C.h_snap, C.d_slots, sizeof(Scalars) * hi, cudaMemcpyDeviceToHost, C.st));
-    SV(cudaEventRecord(C.ev, C.st));
-    C.chunk_in_flight = true;
-    C.steps++;
+    while (C.inflight < 2) {
+        s = launch_chunk(C);
+        if (s != FAST_OK) return s;
+    }
     return FAST_OK;
 }
 
@@ -347,10 +380,12 @@ void destroy(Ctx *C)
     if (C->d_slots) cudaFreeAsync(C->d_slots, C->st);
     if (C->d_cnt) cudaFreeAsync(C->d_cnt, C->st);
     if (C->st) cudaStreamSynchronize(C->st);
-    if (C->h_snap) cudaFreeHost(C->h_snap);
+    for (Scalars *h : C->h_snap)
+        if (h) cudaFreeHost(h);
     if (C->h_init) cudaFreeHost(C->h_init);
     if (C->h_stage) cudaFreeHost(C->h_stage);
-    if (C->ev) cudaEventDestroy(C->ev);
+    for (cudaEvent_t e : C->ev)
+        if (e) cudaEventDestroy(e);
     if (C->st) cudaStreamDestroy(C->st);
     delete C;
 }
@@ -385,7 +420,8 @@ int create(const fast_ctx_config &cfg, Ctx **out)
         return st;
     };
     if (cudaStreamCreateWithFlags(&C->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&C->ev, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&C->ev[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&C->ev[1], cudaEventDisableTiming) != cudaSuccess)
         return fin(ft_fail(FAST_CUDA_ERROR, "stream/event creation failed"));
     if (cudaMallocAsync((void **)&C->d_slots, sizeof(Scalars) * K, C->st) != cudaSuccess ||
         cudaMallocAsync((void **)&C->d_cnt, sizeof(uint32_t) * K, C->st) != cudaSuccess ||
@@ -396,7 +432,8 @@ int create(const fast_ctx_config &cfg, Ctx **out)
         cudaMallocAsync((void **)&C->d_tmp[2], sizeof(Job) * K, C->st) != cudaSuccess)
         return fin(ft_fail(FAST_NOMEM, "context tables"));
     if (cudaMemsetAsync(C->d_cnt, 0, sizeof(uint32_t) * K, C->st) != cudaSuccess ||
-        cudaMallocHost(&C->h_snap, sizeof(Scalars) * K) != cudaSuccess ||
+        cudaMallocHost(&C->h_snap[0], sizeof(Scalars) * K) != cudaSuccess ||
+        cudaMallocHost(&C->h_snap[1], sizeof(Scalars) * K) != cudaSuccess ||
         cudaMallocHost(&C->h_init, sizeof(Scalars) * K) != cudaSuccess ||
         cudaMallocHost(&C->h_stage, sizeof(Job) * 6 * K) != cudaSuccess)
         return fin(ft_fail(FAST_NOMEM, "context staging"));

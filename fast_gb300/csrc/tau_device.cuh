@@ -16,13 +16,29 @@ namespace ft {
 
 // ---------------------------------------------------------------------------
 // Coefficient tables, staged in shared memory at block start.
+//
+// The FP32 iterations of a MIXED solve look up the diagonal of EVERY voxel in
+// a table indexed by its
+// stencil code and its boundary count bc = (missing secondary-axis
+// neighbours) - (missing primary-axis neighbours), bc in [-2, 4]: a missing
+// neighbour's code bit repeats the voxel's own bit, so the interior entry
+// counts D_self for it, which a zero-flux face must give back (+D_self) and a
+// Dirichlet face must double (-D_self: 2*D_self in all).  The count is fixed
+// per thread in x and y for a whole slab and changes only on the first and
+// last plane in z, so the lookup has no branch.  FP64 solves and the
+// reference's FP32 mode keep the coordinate-aware evaluation in the
+// reference's subtraction order for voxels on a domain face (row 2 of the FP32
+// table is the interior diagonal they use).
 // ---------------------------------------------------------------------------
+constexpr int NBC = 7;  // boundary counts -2..4
+
 template <typename T>
 struct Coef {
+    static constexpr int NB = sizeof(T) == 4 ? NBC : 1;
     T face[2][2];      // face coefficient by (self solid, neighbour solid)
     T cell2[2];        // 2*D: the half-cell Dirichlet face (dist = h/2)
-    T diag_int[128];   // diagonal of an interior voxel, by code
-    T inv_int[128];    // its reciprocal
+    T diag_b[NB][128]; // diagonal by (boundary count + 2, code); FP64: interior row only
+    T inv_b[NB][128];  // its reciprocal
 };
 
 template <typename T>
@@ -30,20 +46,38 @@ __device__ __forceinline__ void load_coef(Coef<T> &C, const Job &J, int tid)
 {
     if constexpr (sizeof(T) == 8) {
         if (tid < 128) {
-            C.diag_int[tid] = J.ddiag_int[tid];
-            C.inv_int[tid] = J.dinv_int[tid];
+            C.diag_b[0][tid] = J.ddiag_int[tid];
+            C.inv_b[0][tid] = J.dinv_int[tid];
         }
         if (tid < 4) C.face[tid >> 1][tid & 1] = J.dface[tid >> 1][tid & 1];
         if (tid < 2) C.cell2[tid] = 2.0 * J.dcell[tid];
     } else {
-        if (tid < 128) {
-            C.diag_int[tid] = J.fdiag_int[tid];
-            C.inv_int[tid] = J.finv_int[tid];
+        for (int k = tid; k < NBC * 128; k += NTHREADS) {
+            C.diag_b[k >> 7][k & 127] = J.fdiag_b[k >> 7][k & 127];
+            C.inv_b[k >> 7][k & 127] = J.finv_b[k >> 7][k & 127];
         }
         if (tid < 4) C.face[tid >> 1][tid & 1] = J.fface[tid >> 1][tid & 1];
         if (tid < 2) C.cell2[tid] = (float)(2.0 * J.dcell[tid]);
     }
 }
+
+// Face coefficients of a solve, held in registers by every thread.
+template <typename T>
+struct Faces {
+    T a0, b0, a1, b1;  // (self pore: neighbour pore, solid), (self solid: pore, solid)
+};
+
+template <typename T>
+__device__ __forceinline__ Faces<T> faces_of(const Job &J)
+{
+    if constexpr (sizeof(T) == 8) return Faces<T>{J.dface[0][0], J.dface[0][1], J.dface[1][0], J.dface[1][1]};
+    else return Faces<T>{J.fface[0][0], J.fface[0][1], J.fface[1][0], J.fface[1][1]};
+}
+
+// A voxel of a sweep: coordinates and its boundary count (see above).
+struct Pos {
+    int x, y, z, bc;
+};
 
 struct Geo {
     int nx, ny, nz;
@@ -66,6 +100,20 @@ struct Geo {
     __device__ __forceinline__ int extent() const { return k == 0 ? nx : (k == 1 ? ny : nz); }
 };
 
+// Boundary count contributions: in x and y (fixed per thread for a slab)
+// and in z (per plane).
+__device__ __forceinline__ int boundary_count_xy(const Geo &g, int x, int y)
+{
+    const int mx = (x == 0) + (x == g.nx - 1), my = (y == 0) + (y == g.ny - 1);
+    return (g.k == 0 ? -mx : mx) + (g.k == 1 ? -my : my);
+}
+
+__device__ __forceinline__ int boundary_count_z(const Geo &g, int z)
+{
+    const int mz = (z == 0) + (z == g.nz - 1);
+    return g.k == 2 ? -mz : mz;
+}
+
 // Diagonal of voxel (x,y,z): 0 - c(X+) - c(X-) - c(Y+) - c(Y-) - c(Z+) - c(Z-),
 // the subtraction order of getSystemTopKernel (Diffusion.cuh:85-105).  A
 // face to an in-domain neighbour contributes its face coefficient; a domain
@@ -85,21 +133,45 @@ __device__ __forceinline__ T diag_general(const Coef<T> &C, const Geo &g, uint32
     return d;
 }
 
-// Diagonal and its inverse: table lookups for a voxel with all six
-// neighbours inside the domain, the coordinate-aware evaluation for a voxel
-// on a domain face (BND_BIT of its code).
+// Diagonal and its inverse of the voxel at p.  FAST (the FP32 iterations of
+// a MIXED solve): the boundary-count table, no branch.  Otherwise (FP64 and
+// the reference's FP32 mode): the interior table, or the coordinate-aware
+// evaluation in the reference's subtraction order for a voxel on a domain
+// face (BND_BIT of its code).
 template <typename T>
-__device__ __forceinline__ T diag_of(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+__host__ __device__ constexpr int interior_row() { return Coef<T>::NB == 1 ? 0 : 2; }
+
+template <typename T, bool FAST>
+__device__ __forceinline__ T diag_of(const Coef<T> &C, const Geo &g, uint32_t code, const Pos &p)
 {
-    if (code & (1u << BND_BIT)) return diag_general(C, g, code, x, y, z);
-    return C.diag_int[code & 127];
+    if constexpr (FAST) {
+        return C.diag_b[p.bc + 2][code & 127];
+    } else {
+        if (code & (1u << BND_BIT)) return diag_general(C, g, code, p.x, p.y, p.z);
+        return C.diag_b[interior_row<T>()][code & 127];
+    }
 }
 
-template <typename T>
-__device__ __forceinline__ T inv_of(const Coef<T> &C, const Geo &g, uint32_t code, int x, int y, int z)
+template <typename T, bool FAST>
+__device__ __forceinline__ T inv_of(const Coef<T> &C, const Geo &g, uint32_t code, const Pos &p)
 {
-    if (code & (1u << BND_BIT)) return T(1) / diag_general(C, g, code, x, y, z);
-    return C.inv_int[code & 127];
+    if constexpr (FAST) {
+        return C.inv_b[p.bc + 2][code & 127];
+    } else {
+        if (code & (1u << BND_BIT)) return T(1) / diag_general(C, g, code, p.x, p.y, p.z);
+        return C.inv_b[interior_row<T>()][code & 127];
+    }
+}
+
+// The inverse when the diagonal d of the voxel is already at hand.
+template <typename T, bool FAST>
+__device__ __forceinline__ T inv_from_diag(const Coef<T> &C, uint32_t code, const Pos &p, T d)
+{
+    if constexpr (FAST) {
+        return C.inv_b[p.bc + 2][code & 127];
+    } else {
+        return (code & (1u << BND_BIT)) ? T(1) / d : C.inv_b[interior_row<T>()][code & 127];
+    }
 }
 
 // Right-hand side b (Diffusion.cuh:108-122): on the first plane of the
@@ -132,11 +204,11 @@ __device__ __forceinline__ T x0_at(const Geo &g, int x, int y, int z)
 // just as the reference's zeroed boundary coefficient does; no bounds test is
 // needed.
 template <typename T>
-__device__ __forceinline__ T stencil7(const Coef<T> &C, uint32_t code, T fc, T fxp, T fxm, T fyp, T fym, T fzp,
+__device__ __forceinline__ T stencil7(const Faces<T> &F, uint32_t code, T fc, T fxp, T fxm, T fyp, T fym, T fzp,
                                       T fzm, T diag)
 {
-    const int self = (code >> SELF_BIT) & 1;
-    const T a = C.face[self][0], b = C.face[self][1];
+    const bool solid = (code >> SELF_BIT) & 1;
+    const T a = solid ? F.a1 : F.a0, b = solid ? F.b1 : F.b0;
     T s = fxp * ((code & 1) ? b : a);
     s += fxm * ((code & 2) ? b : a);
     s += fyp * ((code & 4) ? b : a);

@@ -34,15 +34,20 @@ struct Geometry {
     int zc, tx, ty, tz;
     int64_t ntiles;
 };
-Geometry make_geometry(int64_t nx, int64_t ny, int64_t nz);
+constexpr int kSlabDepth = 32;   // planes per block (full size)
+constexpr int kMinBlocks = 608;  // 4 blocks per SM on 152 SMs
+// zc_req > 0: that slab depth; 0: FAST_TAU_ZC or kSlabDepth.
+Geometry make_geometry(int64_t nx, int64_t ny, int64_t nz, int zc_req = 0);
+// The slab depth of a volume's solves (size class; FAST_TAU_ZC overrides).
+int slab_depth(int64_t nx, int64_t ny, int64_t nz);
 size_t align_up(size_t v, size_t a);
 // Row pitch (elements) of every array of a volume: nx rounded up to 16, so a
 // row of any element size starts on a 16-byte boundary (TMA stride rule).
 int64_t row_pitch(int64_t nx);
 
-// Device bytes of one right-hand side (state vectors + partial sums) and of
-// a volume's stencil codes.
-size_t job_bytes(int64_t nx, int64_t ny, int64_t nz, int prec, int solver);
+// Device bytes of one right-hand side (state vectors + partial sums; zc = 0:
+// the volume's slab depth) and of a volume's stencil codes.
+size_t job_bytes(int64_t nx, int64_t ny, int64_t nz, int prec, int solver, int zc = 0);
 size_t code_bytes(int64_t nx, int64_t ny, int64_t nz);
 
 // Bump allocator over one device allocation.
@@ -60,9 +65,10 @@ struct Arena {
 // Fills the descriptor and initial scalars of one right-hand side: state
 // vectors carved from `A`, tensor maps, coefficient tables; `d_sc` and
 // `d_counter` are its device scalars and finisher counter; tile_base is left
-// to the caller.
+// to the caller.  zc = 0: the volume's slab depth.
 int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, int dir,
-              const uint8_t *d_code, Scalars *d_sc, uint32_t *d_counter, Arena &A, const fast_tau_params &P);
+              const uint8_t *d_code, Scalars *d_sc, uint32_t *d_counter, Arena &A, const fast_tau_params &P,
+              int zc = 0);
 
 int status_of(int state);
 int check_params(const fast_tau_params *p);

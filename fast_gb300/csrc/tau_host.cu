@@ -209,21 +209,28 @@ void fill_tables(Job &J, double d0, double d1, int face_mean)
         }
         J.ddiag_int[code] = dd;
         J.dinv_int[code] = 1.0 / dd;
-        J.fdiag_int[code] = df;
-        J.finv_int[code] = 1.0f / df;
+        // FP32 rows by boundary count bc = (missing secondary-axis
+        // neighbours) - (missing primary-axis neighbours): a missing
+        // neighbour's clamped code bit contributed -D_self above; a zero-flux
+        // face contributes 0 and a Dirichlet face -2 D_self.
+        for (int bc = -2; bc <= 4; bc++) {
+            const float d = df + Df[self] * (float)bc;
+            J.fdiag_b[bc + 2][code] = d;
+            J.finv_b[bc + 2][code] = 1.0f / d;
+        }
     }
     J.c_tau[0] = (float)d0;
     J.c_tau[1] = (float)d1;
 }
 
-Geometry make_geometry(int64_t nx, int64_t ny, int64_t nz)
+Geometry make_geometry(int64_t nx, int64_t ny, int64_t nz, int zc_req)
 {
     Geometry g;
     g.nx = nx; g.ny = ny; g.nz = nz;
     g.N = nx * ny * nz;
     g.tx = (int)((nx + TX - 1) / TX);
     g.ty = (int)((ny + TY - 1) / TY);
-    int zc = env_int("FAST_TAU_ZC", 32);
+    int zc = zc_req > 0 ? zc_req : env_int("FAST_TAU_ZC", kSlabDepth);
     if (zc < 1) zc = 1;
     if (zc > nz) zc = (int)nz;
     g.zc = zc;
@@ -389,24 +396,53 @@ struct JobSpec {
 
 size_t code_bytes(int64_t nx, int64_t ny, int64_t nz) { return align_up((size_t)(row_pitch(nx) * ny * nz), 256); }
 
-size_t job_bytes(int64_t nx, int64_t ny, int64_t nz, int prec, int solver)
+// Slab depth by size class: the full depth unless the launch would give the
+// GPU fewer than kMinBlocks blocks, then halved (down to 2 planes) until it
+// does.  A small volume otherwise runs as a few long z-marches (a 64^3 volume
+// makes 16 blocks of 32 planes) and is bound by the per-plane latency, not by
+// the work; a launch with many right-hand sides keeps the full depth (fewer
+// halo planes).  slab_depth sizes a volume solved alone (one right-hand side,
+// the serving context's unit); launch_slab_depth a whole launch.
+int slab_depth(int64_t nx, int64_t ny, int64_t nz)
+{
+    const int env = env_int("FAST_TAU_ZC", 0);
+    if (env > 0) return env;
+    int zc = kSlabDepth;
+    while (zc > 2 && make_geometry(nx, ny, nz, zc).ntiles < kMinBlocks) zc /= 2;
+    return zc;
+}
+
+int launch_slab_depth(const std::vector<VolSpec> &vols, const std::vector<JobSpec> &jobs)
+{
+    const int env = env_int("FAST_TAU_ZC", 0);
+    if (env > 0) return env;
+    int zc = kSlabDepth;
+    for (; zc > 2; zc /= 2) {
+        int64_t blocks = 0;
+        for (const JobSpec &j : jobs) blocks += make_geometry(vols[j.vol].nx, vols[j.vol].ny, vols[j.vol].nz, zc).ntiles;
+        if (blocks >= kMinBlocks) break;
+    }
+    return zc;
+}
+
+size_t job_bytes(int64_t nx, int64_t ny, int64_t nz, int prec, int solver, int zc)
 {
     const bool mixed = prec == FAST_PREC_MIXED;
     const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
     const size_t nvec = (solver == FAST_SOLVER_CG) ? 4 : 8;
     const size_t NP = (size_t)(row_pitch(nx) * ny * nz);
-    const Geometry G = make_geometry(nx, ny, nz);
+    const Geometry G = make_geometry(nx, ny, nz, zc > 0 ? zc : slab_depth(nx, ny, nz));
     return nvec * align_up(NP * vec_t, 256) + (mixed ? 2 * align_up(NP * 8, 256) : 0) +
            align_up((size_t)G.ntiles * NPART * sizeof(double), 256);
 }
 
 // Device bytes of a solve: one stencil-code array per volume, the state
 // vectors, partial sums and scalars of every right-hand side.
-size_t solve_bytes(const std::vector<VolSpec> &vols, const std::vector<JobSpec> &jobs, int prec, int solver)
+size_t solve_bytes(const std::vector<VolSpec> &vols, const std::vector<JobSpec> &jobs, int prec, int solver, int zc)
 {
     size_t need = 4096;
     for (const VolSpec &v : vols) need += code_bytes(v.nx, v.ny, v.nz);
-    for (const JobSpec &j : jobs) need += job_bytes(vols[j.vol].nx, vols[j.vol].ny, vols[j.vol].nz, prec, solver);
+    for (const JobSpec &j : jobs) need += job_bytes(vols[j.vol].nx, vols[j.vol].ny, vols[j.vol].nz, prec, solver, zc);
     const size_t nj = jobs.size(), nv = vols.size();
     need += align_up(sizeof(Scalars) * nj, 256) + align_up(sizeof(uint32_t) * nj, 256) +
             align_up(sizeof(Job) * (nj + nv), 256);
@@ -414,12 +450,12 @@ size_t solve_bytes(const std::vector<VolSpec> &vols, const std::vector<JobSpec> 
 }
 
 int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, int dir,
-              const uint8_t *d_code, Scalars *d_sc, uint32_t *d_counter, Arena &A, const fast_tau_params &P)
+              const uint8_t *d_code, Scalars *d_sc, uint32_t *d_counter, Arena &A, const fast_tau_params &P, int zc)
 {
     const int prec = P.precision, solver = P.solver;
     const bool mixed = prec == FAST_PREC_MIXED;
     const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
-    const Geometry G = make_geometry(nx, ny, nz);
+    const Geometry G = make_geometry(nx, ny, nz, zc > 0 ? zc : slab_depth(nx, ny, nz));
     const int64_t pitch = row_pitch(nx);
     const int64_t NP = pitch * ny * nz;
     const size_t vbytes = align_up((size_t)NP * vec_t, 256);
@@ -508,7 +544,8 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
 
     // --- memory plan (the reference's fit check, VolumeMeasures.cpp:104-125)
-    const size_t need = solve_bytes(vols, jobs, prec, solver);
+    const int zc = launch_slab_depth(vols, jobs);
+    const size_t need = solve_bytes(vols, jobs, prec, solver, zc);
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
     if (need > free_b) {
@@ -549,7 +586,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     for (int j = 0; j < nj; j++) {
         const VolSpec &V = vols[jobs[j].vol];
         const int bs = build_job(hj[j], hs[j], V.d_mask, V.nx, V.ny, V.nz, jobs[j].dir, d_code[jobs[j].vol], d_sc + j,
-                                 d_cnt + j, A, P);
+                                 d_cnt + j, A, P, zc);
         if (bs != FAST_OK) {
             cudaFreeAsync(A.base, st);
             cudaStreamSynchronize(st);

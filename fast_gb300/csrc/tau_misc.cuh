@@ -29,6 +29,7 @@ struct OpReplace {
     struct Own { uint32_t code; float r0; };
     struct Out { double x; float r; };
     const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
     double *x64n;
     float *r, *r0, *p, *v;
     bool restart;
@@ -50,6 +51,7 @@ struct OpReplace {
     }
     __device__ void init(const Job &J, Shared &)
     {
+        F = faces_of<T>(J);
         const Scalars &sc = *J.sc;
         const int cur = sc.x64_cur;
         const int par = BICG ? (int)(sc.iter & 1) : 0;
@@ -64,21 +66,21 @@ struct OpReplace {
         v = BICG ? (float *)J.v[par] : nullptr;
         restart = sc.replace == 2;
     }
-    __device__ double field(const Geo &, const Coef<double> &, Shared &, const Vals &a, int, int, int) const
+    __device__ double field(const Geo &, const Coef<double> &, Shared &, const Vals &a, const Pos &) const
     {
         return a.x + (double)a.e;
     }
-    __device__ Own own(const Geo &, const Coef<double> &, Shared &, const Vals &a, int, int, int, double &f) const
+    __device__ Own own(const Geo &, const Coef<double> &, Shared &, const Vals &a, const Pos &, double &f) const
     {
         f = a.x + (double)a.e;
         return Own{a.code, a.r0};
     }
-    __device__ Out apply(const Geo &g, const Coef<double> &C, Shared &S, const Own &o, int x_, int y_, int z_,
+    __device__ Out apply(const Geo &g, const Coef<double> &C, Shared &S, const Own &o, const Pos &ps,
                          double fc, double fxp, double fxm, double fyp, double fym, double fzp, double fzm)
     {
-        const double d = diag_of<double>(C, g, o.code, x_, y_, z_);
-        const double ax = stencil7<double>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
-        const double b = rhs_at<double>(C, g, o.code, x_, y_, z_);
+        const double d = diag_of<double, false>(C, g, o.code, ps);
+        const double ax = stencil7<double>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const double b = rhs_at<double>(C, g, o.code, ps.x, ps.y, ps.z);
         const double res = b - ax;
         const float r32 = (float)res;
         const float b32 = (float)b;
@@ -87,7 +89,7 @@ struct OpReplace {
         if constexpr (BICG) {
             a_d.add_prod(restart ? r32 : o.r0, r32);
         } else {
-            const float inv = inv_of<float>(S, g, o.code, x_, y_, z_);
+            const float inv = inv_of<float, true>(S, g, o.code, ps);
             a_d.add_prod(r32, r32 * inv);
         }
         return Out{fc, r32};

@@ -288,6 +288,10 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
     const bool h1 = hin_y && (unsigned)(hgx + 1) < (unsigned)g.nx;
     const Pt p_own{ly + 1, 2 * lp};
     const Pt p_halo{hrow, hgx - x0};
+    // Boundary counts in x and y of the thread's own columns and halo points
+    // (fixed for the slab); the z part is added per plane.
+    const int bc0 = boundary_count_xy(g, gx, gy), bc1 = boundary_count_xy(g, gx + 1, gy);
+    const int hbc0 = boundary_count_xy(g, hgx, hgy), hbc1 = boundary_count_xy(g, hgx + 1, hgy);
 
     T fm0 = T(0), fm1 = T(0), fc0 = T(0), fc1 = T(0), fp0 = T(0), fp1 = T(0);
     typename Op::Own oc0{}, oc1{}, op0{}, op1{};
@@ -308,30 +312,31 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
 #endif
         const unsigned char *stage = sbase + st * SB;
         const bool out_plane = zq >= z0 && zq < z1;
+        const int bcz = boundary_count_z(g, zq);
         {
             V a, b;
             Op::load2(stage, p_own, a, b);
             fp0 = T(0);
             fp1 = T(0);
             if (out_plane) {
-                if (v0) op0 = op.own(g, C, S, a, gx, gy, zq, fp0);
-                if (v1) op1 = op.own(g, C, S, b, gx + 1, gy, zq, fp1);
+                if (v0) op0 = op.own(g, C, S, a, Pos{gx, gy, zq, bc0 + bcz}, fp0);
+                if (v1) op1 = op.own(g, C, S, b, Pos{gx + 1, gy, zq, bc1 + bcz}, fp1);
                 *reinterpret_cast<Pair<T> *>(&fb[zq % 3][ly + 1][2 * lp + 2]) = Pair<T>{fp0, fp1};
             } else {
-                if (v0) fp0 = op.field(g, C, S, a, gx, gy, zq);
-                if (v1) fp1 = op.field(g, C, S, b, gx + 1, gy, zq);
+                if (v0) fp0 = op.field(g, C, S, a, Pos{gx, gy, zq, bc0 + bcz});
+                if (v1) fp1 = op.field(g, C, S, b, Pos{gx + 1, gy, zq, bc1 + bcz});
             }
         }
         if (out_plane && hkind == 1) {
             V a, b;
             Op::load2(stage, p_halo, a, b);
-            const T f0 = h0 ? op.field(g, C, S, a, hgx, hgy, zq) : T(0);
-            const T f1 = h1 ? op.field(g, C, S, b, hgx + 1, hgy, zq) : T(0);
+            const T f0 = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
+            const T f1 = h1 ? op.field(g, C, S, b, Pos{hgx + 1, hgy, zq, hbc1 + bcz}) : T(0);
             *reinterpret_cast<Pair<T> *>(&fb[zq % 3][hrow][hcol]) = Pair<T>{f0, f1};
         } else if (out_plane && hkind == 2) {
             V a;
             Op::load1(stage, p_halo, a);
-            fb[zq % 3][hrow][hcol] = h0 ? op.field(g, C, S, a, hgx, hgy, zq) : T(0);
+            fb[zq % 3][hrow][hcol] = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
         }
         __syncthreads();
         if (s_err) break;
@@ -342,6 +347,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
         }
         const int zs = zq - 1;
         if (zs >= z0 && zs < z1 && (v0 || v1)) {
+            const int bczs = boundary_count_z(g, zs);
             const T(*P)[PW] = fb[zs % 3];
             const Pair<T> left = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp]);
             const Pair<T> right = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp + 4]);
@@ -349,8 +355,8 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
             const Pair<T> dn = *reinterpret_cast<const Pair<T> *>(&P[ly][2 * lp + 2]);
             const int64_t i = i_col + plane * zs;
             typename Op::Out r0{}, r1{};
-            if (v0) r0 = op.apply(g, C, S, oc0, gx, gy, zs, fc0, fc1, left.b, up.a, dn.a, fp0, fm0);
-            if (v1) r1 = op.apply(g, C, S, oc1, gx + 1, gy, zs, fc1, right.a, fc0, up.b, dn.b, fp1, fm1);
+            if (v0) r0 = op.apply(g, C, S, oc0, Pos{gx, gy, zs, bc0 + bczs}, fc0, fc1, left.b, up.a, dn.a, fp0, fm0);
+            if (v1) r1 = op.apply(g, C, S, oc1, Pos{gx + 1, gy, zs, bc1 + bczs}, fc1, right.a, fc0, up.b, dn.b, fp1, fm1);
             op.store(i, r0, r1, v0, v1);
         }
         fm0 = fc0;
@@ -375,14 +381,15 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
     // The last plane of the volume has no z+1 neighbour: apply it here.
     if (pb == z1 - 1 && (v0 || v1)) {
         const int zs = z1 - 1;
+        const int bczs = boundary_count_z(g, zs);
         const T(*P)[PW] = fb[zs % 3];
         const Pair<T> left = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp]);
         const Pair<T> right = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp + 4]);
         const Pair<T> up = *reinterpret_cast<const Pair<T> *>(&P[ly + 2][2 * lp + 2]);
         const Pair<T> dn = *reinterpret_cast<const Pair<T> *>(&P[ly][2 * lp + 2]);
         typename Op::Out r0{}, r1{};
-        if (v0) r0 = op.apply(g, C, S, oc0, gx, gy, zs, fc0, fc1, left.b, up.a, dn.a, T(0), fm0);
-        if (v1) r1 = op.apply(g, C, S, oc1, gx + 1, gy, zs, fc1, right.a, fc0, up.b, dn.b, T(0), fm1);
+        if (v0) r0 = op.apply(g, C, S, oc0, Pos{gx, gy, zs, bc0 + bczs}, fc0, fc1, left.b, up.a, dn.a, T(0), fm0);
+        if (v1) r1 = op.apply(g, C, S, oc1, Pos{gx + 1, gy, zs, bc1 + bczs}, fc1, right.a, fc0, up.b, dn.b, T(0), fm1);
         op.store(i_col + plane * zs, r0, r1, v0, v1);
     }
 
@@ -429,6 +436,7 @@ __device__ __forceinline__ void load_code2(const unsigned char *st, const Pt &p,
 template <typename TT, typename ST, bool BICG>
 struct OpInit {
     using T = TT;
+    static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
     using SL = Streams<1>;
     static constexpr int NV = 3;
     using Shared = NoShared;
@@ -436,6 +444,7 @@ struct OpInit {
     struct Own { uint32_t code; };
     struct Out { T x, r; };
     const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
     T *x, *r, *r0, *p0, *v0;
     Acc<T> bb, rr, rz;
 
@@ -448,26 +457,27 @@ struct OpInit {
     __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a) { a.code = sv<uint8_t, SL, 0>(st, p); }
     __device__ void init(const Job &J, Shared &)
     {
+        F = faces_of<T>(J);
         tmap[0] = &J.tm[TM_CODE];
         x = (T *)J.x; r = (T *)J.r[0]; r0 = (T *)J.r0; p0 = (T *)J.p[0]; v0 = (T *)J.v[0];
     }
-    __device__ T field(const Geo &g, const Coef<T> &, Shared &, const Vals &, int x_, int y_, int z_) const
+    __device__ T field(const Geo &g, const Coef<T> &, Shared &, const Vals &, const Pos &ps) const
     {
-        return x0_at<T>(g, x_, y_, z_);
+        return x0_at<T>(g, ps.x, ps.y, ps.z);
     }
-    __device__ Own own(const Geo &g, const Coef<T> &, Shared &, const Vals &v, int x_, int y_, int z_, T &f) const
+    __device__ Own own(const Geo &g, const Coef<T> &, Shared &, const Vals &v, const Pos &ps, T &f) const
     {
-        f = x0_at<T>(g, x_, y_, z_);
+        f = x0_at<T>(g, ps.x, ps.y, ps.z);
         return Own{v.code};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
-        const T ax = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
-        const T b = rhs_at<T>(C, g, o.code, x_, y_, z_);
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T ax = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T b = rhs_at<T>(C, g, o.code, ps.x, ps.y, ps.z);
         const T res = b - ax;
-        const T inv = (o.code & (1u << BND_BIT)) ? T(1) / d : C.inv_int[o.code & 127];
+        const T inv = inv_from_diag<T, FB>(C, o.code, ps, d);
         bb.add_prod(b, b);
         rr.add_prod(res, res);
         rz.add_prod(res, res * inv);
@@ -582,6 +592,7 @@ __device__ __forceinline__ void mixed_bicg_finish(Scalars &sc, double r0r, doubl
 template <typename TT, typename ST>
 struct OpCG1 {
     using T = TT;
+    static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
     using SL = Streams<sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 1;
     using Shared = NoShared;
@@ -589,6 +600,7 @@ struct OpCG1 {
     struct Own { uint32_t code; };
     struct Out { T p; };
     const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
     T *pnew;
     T *ezero;  // MIXED: e to zero after a residual replacement, else null
     T beta;
@@ -610,6 +622,7 @@ struct OpCG1 {
     }
     __device__ void init(const Job &J, Shared &)
     {
+        F = faces_of<T>(J);
         const int par = (int)(J.sc->iter & 1);
         tmap[0] = &J.tm[TM_R];
         tmap[1] = &J.tm[TM_P + par];
@@ -618,21 +631,21 @@ struct OpCG1 {
         ezero = J.sc->e_reset ? (T *)J.x : nullptr;
         beta = (T)J.sc->beta;
     }
-    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_) const
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps) const
     {
-        const T zi = v.r * inv_of<T>(C, g, v.code, x_, y_, z_);
+        const T zi = v.r * inv_of<T, FB>(C, g, v.code, ps);
         return v.p * beta + zi;  // __aAddAlphaBKernel: p = p*beta + z
     }
-    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &S, const Vals &v, int x_, int y_, int z_, T &f) const
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &S, const Vals &v, const Pos &ps, T &f) const
     {
-        f = field(g, C, S, v, x_, y_, z_);
+        f = field(g, C, S, v, ps);
         return Own{v.code};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
-        const T q = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T q = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         pap.add_prod(fc, q);
         return Out{fc};
     }
@@ -657,6 +670,7 @@ struct OpCG1 {
 template <typename TT, typename ST>
 struct OpCG2 {
     using T = TT;
+    static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
     using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 2;
     using Shared = NoShared;
@@ -664,6 +678,7 @@ struct OpCG2 {
     struct Own { uint32_t code; T x, r; };
     struct Out { T x, r; };
     const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
     T *x, *r;
     T alpha;
     Acc<T> rr, rz;
@@ -680,6 +695,7 @@ struct OpCG2 {
     __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a) { a.p = sv<T, SL, 0>(st, p); }
     __device__ void init(const Job &J, Shared &)
     {
+        F = faces_of<T>(J);
         const int par = (int)(J.sc->iter & 1);
         tmap[0] = &J.tm[TM_P + (par ^ 1)];
         tmap[1] = &J.tm[TM_X];
@@ -689,20 +705,20 @@ struct OpCG2 {
         r = (T *)J.r[0];
         alpha = (T)J.sc->alpha;
     }
-    __device__ T field(const Geo &, const Coef<T> &, Shared &, const Vals &v, int, int, int) const { return v.p; }
-    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const Vals &v, int, int, int, T &f) const
+    __device__ T field(const Geo &, const Coef<T> &, Shared &, const Vals &v, const Pos &) const { return v.p; }
+    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const Vals &v, const Pos &, T &f) const
     {
         f = v.p;
         return Own{v.code, v.x, v.r};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
-        const T q = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T q = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         const T xn = o.x + alpha * fc;        // __aAddBetaBKernel(x, p, alpha)
         const T rn = o.r + (-alpha) * q;      // __aAddBetaBKernel(r, ap, -alpha)
-        const T inv = (o.code & (1u << BND_BIT)) ? T(1) / d : C.inv_int[o.code & 127];
+        const T inv = inv_from_diag<T, FB>(C, o.code, ps, d);
         rr.add_prod(rn, rn);
         rz.add_prod(rn, rn * inv);
         return Out{xn, rn};
@@ -742,6 +758,7 @@ struct OpCG2 {
 template <typename TT, typename ST>
 struct OpBiRestart {
     using T = TT;
+    static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
     using SL = Streams<sizeof(TT), 1>;
     static constexpr int NV = 1;
     using Shared = NoShared;
@@ -749,6 +766,7 @@ struct OpBiRestart {
     struct Own { uint32_t code; };
     struct Out { T r; };
     const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
     T *r, *r0;
     Acc<T> rr;
 
@@ -762,24 +780,25 @@ struct OpBiRestart {
     __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a) { a.x = sv<T, SL, 0>(st, p); }
     __device__ void init(const Job &J, Shared &)
     {
+        F = faces_of<T>(J);
         const int par = (int)(J.sc->iter & 1);
         tmap[0] = &J.tm[TM_X];
         tmap[1] = &J.tm[TM_CODE];
         r = (T *)J.r[par];
         r0 = (T *)J.r0;
     }
-    __device__ T field(const Geo &, const Coef<T> &, Shared &, const Vals &v, int, int, int) const { return v.x; }
-    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const Vals &v, int, int, int, T &f) const
+    __device__ T field(const Geo &, const Coef<T> &, Shared &, const Vals &v, const Pos &) const { return v.x; }
+    __device__ Own own(const Geo &, const Coef<T> &, Shared &, const Vals &v, const Pos &, T &f) const
     {
         f = v.x;
         return Own{v.code};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
-        const T ax = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
-        const T res = rhs_at<T>(C, g, o.code, x_, y_, z_) - ax;
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T ax = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T res = rhs_at<T>(C, g, o.code, ps.x, ps.y, ps.z) - ax;
         rr.add_prod(res, res);
         return Out{res};
     }
@@ -808,6 +827,7 @@ struct OpBiRestart {
 template <typename TT, typename ST>
 struct OpBi1 {
     using T = TT;
+    static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
     using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 1;
     using Shared = NoShared;
@@ -815,6 +835,7 @@ struct OpBi1 {
     struct Own { uint32_t code; T p, r0; };
     struct Out { T p, v; };
     const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
     T *pnew, *vnew;
     T *ezero;  // MIXED: e to zero after a residual replacement, else null
     T beta, nw;
@@ -839,6 +860,7 @@ struct OpBi1 {
     }
     __device__ void init(const Job &J, Shared &)
     {
+        F = faces_of<T>(J);
         const int par = (int)(J.sc->iter & 1);
         tmap[0] = &J.tm[TM_R + par];
         tmap[1] = &J.tm[TM_P + par];
@@ -853,21 +875,21 @@ struct OpBi1 {
     }
     // __aPlusBetaBGammaPlusCKernel: p = beta*(p + (-w)*v) + r
     __device__ __forceinline__ T pval(const Vals &v) const { return beta * (v.p + nw * v.v) + v.r; }
-    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_) const
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps) const
     {
-        return pval(v) * inv_of<T>(C, g, v.code, x_, y_, z_);
+        return pval(v) * inv_of<T, FB>(C, g, v.code, ps);
     }
-    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_, T &f) const
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps, T &f) const
     {
         const T pn = pval(v);
-        f = pn * inv_of<T>(C, g, v.code, x_, y_, z_);
+        f = pn * inv_of<T, FB>(C, g, v.code, ps);
         return Own{v.code, pn, v.r0};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
-        const T vn = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T vn = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         r0v.add_prod(o.r0, vn);
         return Out{o.p, vn};
     }
@@ -892,6 +914,7 @@ struct OpBi1 {
 template <typename TT, typename ST>
 struct OpBi2 {
     using T = TT;
+    static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
     using SL = Streams<sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 2;
     using Shared = NoShared;
@@ -899,6 +922,7 @@ struct OpBi2 {
     struct Own { uint32_t code; T s; };
     using Out = NoOut;
     const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
     T nalpha;
     Acc<T> ts, tt;
 
@@ -918,6 +942,7 @@ struct OpBi2 {
     }
     __device__ void init(const Job &J, Shared &)
     {
+        F = faces_of<T>(J);
         const int par = (int)(J.sc->iter & 1);
         tmap[0] = &J.tm[TM_R + par];
         tmap[1] = &J.tm[TM_V + (par ^ 1)];
@@ -925,21 +950,21 @@ struct OpBi2 {
         nalpha = (T)(-J.sc->alpha);
     }
     __device__ __forceinline__ T sval(const Vals &v) const { return v.r + nalpha * v.v; }  // s = r + (-alpha) v
-    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_) const
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps) const
     {
-        return sval(v) * inv_of<T>(C, g, v.code, x_, y_, z_);
+        return sval(v) * inv_of<T, FB>(C, g, v.code, ps);
     }
-    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_, T &f) const
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps, T &f) const
     {
         const T s = sval(v);
-        f = s * inv_of<T>(C, g, v.code, x_, y_, z_);
+        f = s * inv_of<T, FB>(C, g, v.code, ps);
         return Own{v.code, s};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
-        const T t = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T t = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         ts.add_prod(t, o.s);
         tt.add_prod(t, t);
         return Out{};
@@ -962,6 +987,7 @@ struct OpBi2 {
 template <typename TT, typename ST>
 struct OpBi3 {
     using T = TT;
+    static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
     using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 2;
     using Shared = NoShared;
@@ -969,6 +995,7 @@ struct OpBi3 {
     struct Own { uint32_t code; T s, x, y, r0; };
     struct Out { T x, r; };
     const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
     T *x, *rnew;
     T alpha, omega, nalpha, nomega;
     Acc<T> r0r, rr;
@@ -992,6 +1019,7 @@ struct OpBi3 {
     }
     __device__ void init(const Job &J, Shared &)
     {
+        F = faces_of<T>(J);
         const int par = (int)(J.sc->iter & 1);
         tmap[0] = &J.tm[TM_R + par];
         tmap[1] = &J.tm[TM_V + (par ^ 1)];
@@ -1007,22 +1035,22 @@ struct OpBi3 {
         nomega = -omega;
     }
     __device__ __forceinline__ T sval(const Vals &v) const { return v.r + nalpha * v.v; }
-    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_) const
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps) const
     {
-        return sval(v) * inv_of<T>(C, g, v.code, x_, y_, z_);
+        return sval(v) * inv_of<T, FB>(C, g, v.code, ps);
     }
-    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, int x_, int y_, int z_, T &f) const
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps, T &f) const
     {
         const T s = sval(v);
-        const T inv = inv_of<T>(C, g, v.code, x_, y_, z_);
+        const T inv = inv_of<T, FB>(C, g, v.code, ps);
         f = s * inv;
         return Own{v.code, s, v.x, v.p * inv, v.r0};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, int x_, int y_, int z_, T fc,
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_of<T>(C, g, o.code, x_, y_, z_);
-        const T t = stencil7<T>(C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T t = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         const T xn = o.x + (alpha * o.y + omega * fc);   // __ABC_BetaGammaKernel: x += a*y + w*z
         const T rn = o.s + nomega * t;                   // __aPlusBetaBKernel(s, t, r, -w)
         r0r.add_prod(o.r0, rn);

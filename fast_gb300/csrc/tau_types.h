@@ -107,8 +107,8 @@ struct Job {
     double dface[2][2];          // face coefficient by (self solid, neighbour solid)
     double dcell[2];             // cell diffusivity by solid bit (pore, solid)
     float fface[2][2];
-    float fdiag_int[128];        // interior diagonal by code (7 bits), FP32
-    float finv_int[128];         // 1/diag, FP32
+    float fdiag_b[7][128];       // FP32 diagonal by (boundary count + 2, code 7 bits)
+    float finv_b[7][128];        // 1/diag, FP32
     double ddiag_int[128];       // interior diagonal, FP64
     double dinv_int[128];        // 1/diag, FP64
     float c_tau[2];              // tau cell coefficients (float coeffs of the reference)

@@ -285,7 +285,9 @@ def solve_batch(volumes: Sequence, params: TortuosityParams,
     """Many volumes in one call (fast_tau_solve_batch): ``volumes`` is a
     sequence of (mask, dir) pairs, masks 3-D uint8 [z, y, x] of any sizes.
     Every right-hand side advances in the same launches and retires as soon
-    as it converges; each result equals solving that volume alone."""
+    as it converges; each result equals solving that volume alone up to the
+    summation order of its dot products (the slab depth is chosen for the
+    whole launch)."""
     masks, dirs = [], []
     for mask, d in volumes:
         m = _as_mask(mask)

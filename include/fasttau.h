@@ -147,9 +147,11 @@ typedef struct fast_tau_volume {
 /* Many volumes of different sizes in one call (no counterpart in the
  * reference, which solves one volume per getTortuosity call): all right-hand
  * sides advance together, one launch per solver step covering every
- * (volume, tile) pair, and each is retired as soon as it converges.  Results
- * are identical to solving each volume alone (the reductions of a right-hand
- * side never mix with another's).  1..1024 volumes; p->dir is ignored.
+ * (volume, tile) pair, and each is retired as soon as it converges.  The
+ * reductions of a right-hand side never mix with another's; a result equals
+ * solving the volume alone up to the summation order of its dot products,
+ * which follows the slab depth (chosen for the whole launch by its size; a
+ * volume alone may get a shallower one).  1..1024 volumes; p->dir is ignored.
  * Returns the first non-OK status. */
 FAST_API int fast_tau_solve_batch(const fast_tau_volume *vols, int32_t nvols, const fast_tau_params *p,
                                   fast_tau_result *results);

@@ -1,6 +1,7 @@
 """Batched solves of uneven volumes (fast_tau_solve_batch): every right-hand
-side of the batch must give exactly what it gives alone (its reductions never
-mix with another's), and match the oracle within the single-solve bounds."""
+side of the batch gives what it gives alone (bit-identical at a fixed slab
+depth: its reductions never mix with another's), and matches the oracle
+within the single-solve bounds."""
 import numpy as np
 import pytest
 
@@ -24,15 +25,31 @@ def _batch(seed, n=7):
 @pytest.mark.parametrize("solver", [ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB])
 @pytest.mark.parametrize("prec", [ft.Precision.F64, ft.Precision.MIXED])
 def test_batch_equals_single(gpu, solver, prec):
+    # A batch picks its slab depth for the whole launch, a volume solved alone
+    # for itself, so the two differ only in the order of the dot-product
+    # partial sums: equal within the rounding of a tol-1e-8 solve.
     vols = _batch(100 + int(prec) * 2 + int(solver))
     p = ft.TortuosityParams(tolerance=1e-8, precision=prec)
     batch = ft.solve_batch(vols, p, solver)
     assert len(batch) == len(vols)
     for (m, d), r in zip(vols, batch):
         single = ft.solve_directions(m, [d], p, solver)[0]
-        assert r.status == single.status
-        assert (r.tau, r.iterations, r.outer_steps, r.porosity) == \
-            (single.tau, single.iterations, single.outer_steps, single.porosity)
+        assert r.status == single.status == ft.Status.OK
+        assert r.porosity == single.porosity
+        assert abs(r.tau - single.tau) <= 1e-6 * single.tau
+
+
+def test_batch_is_bit_identical_at_fixed_depth(gpu, monkeypatch):
+    # With the slab depth fixed, the right-hand sides of a batch never mix:
+    # every result is bit-identical to the volume solved alone.
+    monkeypatch.setenv("FAST_TAU_ZC", "8")
+    vols = _batch(77, n=5)
+    for solver in (ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB):
+        p = ft.TortuosityParams(tolerance=1e-8, precision=ft.Precision.MIXED)
+        batch = ft.solve_batch(vols, p, solver)
+        for (m, d), r in zip(vols, batch):
+            single = ft.solve_directions(m, [d], p, solver)[0]
+            assert (r.tau, r.iterations, r.outer_steps) == (single.tau, single.iterations, single.outer_steps)
 
 
 def test_batch_matches_oracle(gpu, oracle):
