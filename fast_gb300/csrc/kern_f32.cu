@@ -61,10 +61,18 @@ static cudaError_t configure()
 cudaError_t configure_f32()
 {
     cudaError_t a = configure<float>(), b = configure<double>();
-    return a != cudaSuccess ? a : b;
+    cudaError_t c = cfg<OpBiK1>(), d = cfg<OpBiK2>();
+    if (a != cudaSuccess) return a;
+    if (b != cudaSuccess) return b;
+    return c != cudaSuccess ? c : d;
 }
 
 void launch_pure_f32(Step s, const Launch &L, cudaStream_t st) { dispatch<float>(s, L, st); }
-void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st) { dispatch<double>(s, L, st); }
+void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st)
+{
+    if (s == Step::BI_K1) go<OpBiK1>(L, st);
+    else if (s == Step::BI_K2) go<OpBiK2>(L, st);
+    else dispatch<double>(s, L, st);
+}
 
 }  // namespace ft

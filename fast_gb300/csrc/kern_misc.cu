@@ -9,8 +9,8 @@ constexpr int kStages = 3;
 void launch_replace(bool bicg, const Launch &L, cudaStream_t st)
 {
     if (bicg)
-        sweep_kernel<OpReplace<true>, kStages>
-            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpReplace<true>, kStages>(), st>>>(L);
+        sweep_kernel<OpReplaceBi2, kStages>
+            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpReplaceBi2, kStages>(), st>>>(L);
     else
         sweep_kernel<OpReplace<false>, kStages>
             <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpReplace<false>, kStages>(), st>>>(L);
@@ -18,9 +18,9 @@ void launch_replace(bool bicg, const Launch &L, cudaStream_t st)
 
 cudaError_t configure_misc()
 {
-    cudaError_t a = cudaFuncSetAttribute(sweep_kernel<OpReplace<true>, kStages>,
+    cudaError_t a = cudaFuncSetAttribute(sweep_kernel<OpReplaceBi2, kStages>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         sweep_dyn_smem<OpReplace<true>, kStages>());
+                                         sweep_dyn_smem<OpReplaceBi2, kStages>());
     cudaError_t b = cudaFuncSetAttribute(sweep_kernel<OpReplace<false>, kStages>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          sweep_dyn_smem<OpReplace<false>, kStages>());

@@ -109,7 +109,7 @@ int steps_of(const Ctx &C, int solver, std::vector<Step> &steps)
     if (solver == FAST_SOLVER_CG) {
         steps = mixed ? std::vector<Step>{Step::REPLACE_CG, Step::CG1, Step::CG2} : std::vector<Step>{Step::CG1, Step::CG2};
     } else {
-        steps = mixed ? std::vector<Step>{Step::REPLACE_BI, Step::BI1, Step::BI2, Step::BI3}
+        steps = mixed ? std::vector<Step>{Step::REPLACE_BI, Step::BI_K1, Step::BI_K2}
                       : std::vector<Step>{Step::BI_RESTART, Step::BI1, Step::BI2, Step::BI3};
     }
     return FAST_OK;

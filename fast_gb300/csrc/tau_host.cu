@@ -154,6 +154,8 @@ int kind_of(Step s)
     case Step::BI3: return FAST_K_BI3;
     case Step::REPLACE_CG:
     case Step::REPLACE_BI: return FAST_K_REPLACE;
+    case Step::BI_K1: return FAST_K_BI1;
+    case Step::BI_K2: return FAST_K_BI2;
     }
     return FAST_K_COUNT - 1;
 }
@@ -429,7 +431,8 @@ size_t job_bytes(int64_t nx, int64_t ny, int64_t nz, int prec, int solver, int z
 {
     const bool mixed = prec == FAST_PREC_MIXED;
     const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
-    const size_t nvec = (solver == FAST_SOLVER_CG) ? 4 : 8;
+    // CG: x, r, p x2; BiCGSTAB: x, r x2, r0, p x2, v x2 (+ t for MIXED)
+    const size_t nvec = (solver == FAST_SOLVER_CG) ? 4 : (mixed ? 9 : 8);
     const size_t NP = (size_t)(row_pitch(nx) * ny * nz);
     const Geometry G = make_geometry(nx, ny, nz, zc > 0 ? zc : slab_depth(nx, ny, nz));
     return nvec * align_up(NP * vec_t, 256) + (mixed ? 2 * align_up(NP * 8, 256) : 0) +
@@ -483,6 +486,7 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     if (mixed) {
         J.x64[0] = (double *)A.take(v64);
         J.x64[1] = (double *)A.take(v64);
+        if (solver == FAST_SOLVER_BICGSTAB) J.t = A.take(vbytes);
     }
     J.part = (double *)A.take((size_t)G.ntiles * NPART * sizeof(double));
     if (A.off > A.cap) return fail(FAST_CUDA_ERROR, "internal: device plan overflow");
@@ -501,6 +505,7 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     if (ts == FAST_OK && mixed) {
         ts = tensor_map(&J.tm[TM_X64], J.x64[0], 8, nx, ny, nz, pitch);
         if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_X64 + 1], J.x64[1], 8, nx, ny, nz, pitch);
+        if (ts == FAST_OK && J.t) ts = tensor_map(&J.tm[TM_T], J.t, 4, nx, ny, nz, pitch);
     }
     if (ts != FAST_OK) return ts;
     J.sc = d_sc;
@@ -524,6 +529,9 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     const double cmin = env_double("FAST_TAU_SHADOW_COS", 1e-4);
     S.cos2_min = cmin * cmin;
     S.inner_mode = mixed ? 1 : 0;
+    // MIXED BiCGSTAB: no update is pending before the first replacement.
+    S.alpha = 0.0;
+    S.omega = 0.0;
     return FAST_OK;
 }
 
@@ -634,7 +642,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
         launch_counted(FAST_K_INIT64, st, [&] { launch_init64(L, st); });
         std::vector<Step> steps;
         if (solver == FAST_SOLVER_CG) steps = {Step::REPLACE_CG, Step::CG1, Step::CG2};
-        else steps = {Step::REPLACE_BI, Step::BI1, Step::BI2, Step::BI3};
+        else steps = {Step::REPLACE_BI, Step::BI_K1, Step::BI_K2};
         status = iterate(E, L, nj, d_sc, steps, dispatch_mixed, P.max_iter);
     }
     if (status == FAST_OK)

@@ -6,13 +6,14 @@
 
 namespace ft {
 
-enum class Step { INIT_CG, INIT_BI, CG1, CG2, BI_RESTART, BI1, BI2, BI3, REPLACE_CG, REPLACE_BI };
+enum class Step { INIT_CG, INIT_BI, CG1, CG2, BI_RESTART, BI1, BI2, BI3, REPLACE_CG, REPLACE_BI, BI_K1, BI_K2 };
 
 // Pure-precision solves: `f64` selects double, otherwise float (scalars in
 // the solve precision, as the reference's T).
 void launch_pure_f64(Step s, const Launch &L, cudaStream_t st);
 void launch_pure_f32(Step s, const Launch &L, cudaStream_t st);
-// FP32 inner iterations of a MIXED solve (scalars in double).
+// FP32 iterations of a MIXED solve (scalars in double); BI_K1/BI_K2 are the
+// two-sweep BiCGSTAB steps, MIXED only.
 void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st);
 // FP64 residual replacement of a MIXED solve (a no-op launch unless the
 // solve asked for one).

@@ -154,6 +154,142 @@ struct OpReplace {
 };
 
 // ===========================================================================
+// MIXED two-sweep BiCGSTAB: the FP64 residual replacement at the head of an
+// iteration.  The updates of the last iteration are still pending (step 1
+// applies them), so the iterate is formed on the fly,
+//   e_k = e + a y + w z, y = p/diag, z = (r - a v)/diag   (FP32, as step 1),
+//   x = x64 + e_k                                          (FP64),
+// at every tile and halo point; then r64 = b - A x in FP64.  x64' = x is
+// stored, fp32(r64) goes to t, from which step 1 takes r_k (k1_mode = 1, e =
+// 0); on a restart it also becomes the shadow residual r0 and beta = 0 makes
+// p_k = r_k.  Dots (FP32-accumulated): |fp32(r64)|^2, |b|^2, r0.fp32(r64).
+// Streams: x64, e, p, r, v, r0, code.
+// ===========================================================================
+struct OpReplaceBi2 {
+    using T = double;
+    using SL = Streams<8, 4, 4, 4, 4, 4, 1>;
+    static constexpr int NV = 3;
+    using Shared = Coef<float>;
+    struct Vals { double x; float e, p, r, v, r0; uint32_t code; };
+    struct Own { uint32_t code; float r0; };
+    struct Out { double x; float r; };
+    const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
+    double *x64n;
+    float *t, *r0;
+    float alpha, omega;
+    bool restart;
+    Acc<float> a_rr, a_bb, a_d;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING && sc.replace != 0; }
+    __device__ static void load_shared(Shared &S, const Job &J, int tid) { load_coef<float>(S, J, tid); }
+    __device__ static void load2(const unsigned char *st, const Pt &p_, Vals &a, Vals &b)
+    {
+        sv2<double, SL, 0>(st, p_, a.x, b.x);
+        sv2<float, SL, 1>(st, p_, a.e, b.e);
+        sv2<float, SL, 2>(st, p_, a.p, b.p);
+        sv2<float, SL, 3>(st, p_, a.r, b.r);
+        sv2<float, SL, 4>(st, p_, a.v, b.v);
+        sv2<float, SL, 5>(st, p_, a.r0, b.r0);
+        load_code2<SL, 6>(st, p_, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p_, Vals &a)
+    {
+        a.x = sv<double, SL, 0>(st, p_);
+        a.e = sv<float, SL, 1>(st, p_);
+        a.p = sv<float, SL, 2>(st, p_);
+        a.r = sv<float, SL, 3>(st, p_);
+        a.v = sv<float, SL, 4>(st, p_);
+        a.code = sv<uint8_t, SL, 6>(st, p_);
+    }
+    __device__ void init(const Job &J, Shared &)
+    {
+        F = faces_of<T>(J);
+        const Scalars &sc = *J.sc;
+        const int cur = sc.x64_cur;
+        const int par = (int)(sc.iter & 1);
+        tmap[0] = &J.tm[TM_X64 + cur];
+        tmap[1] = &J.tm[TM_X];
+        tmap[2] = &J.tm[TM_P + par];
+        tmap[3] = &J.tm[TM_R + par];
+        tmap[4] = &J.tm[TM_V + par];
+        tmap[5] = &J.tm[TM_R0];
+        tmap[6] = &J.tm[TM_CODE];
+        x64n = J.x64[cur ^ 1];
+        t = (float *)J.t;
+        r0 = (float *)J.r0;
+        alpha = (float)sc.alpha;
+        omega = (float)sc.omega;
+        restart = sc.replace == 2;
+    }
+    __device__ double iterate(const Geo &g, Shared &S, const Vals &a, const Pos &ps) const
+    {
+        const float inv = inv_of<float, true>(S, g, a.code, ps);
+        const float ek = a.e + alpha * (a.p * inv) + omega * ((a.r - alpha * a.v) * inv);
+        return a.x + (double)ek;
+    }
+    __device__ double field(const Geo &g, const Coef<double> &, Shared &S, const Vals &a, const Pos &ps) const
+    {
+        return iterate(g, S, a, ps);
+    }
+    __device__ Own own(const Geo &g, const Coef<double> &, Shared &S, const Vals &a, const Pos &ps, double &f) const
+    {
+        f = iterate(g, S, a, ps);
+        return Own{a.code, a.r0};
+    }
+    __device__ Out apply(const Geo &g, const Coef<double> &C, Shared &, const Own &o, const Pos &ps, double fc,
+                         double fxp, double fxm, double fyp, double fym, double fzp, double fzm)
+    {
+        const double d = diag_of<double, false>(C, g, o.code, ps);
+        const double ax = stencil7<double>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const double b = rhs_at<double>(C, g, o.code, ps.x, ps.y, ps.z);
+        const float r32 = (float)(b - ax);
+        const float b32 = (float)b;
+        a_rr.add_prod(r32, r32);
+        a_bb.add_prod(b32, b32);
+        a_d.add_prod(restart ? r32 : o.r0, r32);
+        return Out{fc, r32};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0_, bool v1_)
+    {
+        store2<double>(x64n, i, a.x, b.x, v0_, v1_);
+        store2<float>(t, i, a.r, b.r, v0_, v1_);
+        if (restart) store2<float>(r0, i, a.r, b.r, v0_, v1_);
+    }
+    __device__ void partials(double (&v)[NV]) const
+    {
+        v[0] = (double)a_rr.hi(); v[1] = (double)a_bb.hi(); v[2] = (double)a_d.hi();
+    }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV])
+    {
+        const int mode = sc.replace;
+        sc.replace = 0;
+        sc.b64_sq = t[1];
+        if (t[1] == 0.0) { sc.state = ZERO_RHS; return; }
+        sc.x64_cur ^= 1;
+        sc.k1_mode = 1;
+        sc.outer_steps += 1;
+        sc.r64_sq = t[0];
+        const double tol2 = sc.tol_outer * sc.tol_outer * t[1];
+        sc.tol2 = tol2;
+        sc.rhs_sq = t[1];
+        if (t[0] <= tol2) { sc.state = CONVERGED; return; }
+        if (!(t[0] <= sc.div_thresh)) { sc.state = DIVERGED; return; }  // also NaN
+        if (sc.iter >= sc.max_iter) { sc.state = MAXITER; return; }
+        sc.rsq = t[0];
+        sc.rsq_max = t[0];
+        if (mode == 2) {  // new shadow residual r0 = r: rho = |r|^2, p_k = r_k
+            sc.r0_sq = t[0];
+            sc.rho = t[0];
+            sc.beta = 0.0;
+        } else {          // rho_old, alpha, omega are those of the last iteration
+            sc.rho = t[2];
+            sc.beta = (t[2] / sc.rho_old) * (sc.alpha / sc.omega);
+        }
+    }
+};
+
+// ===========================================================================
 // Pointwise kernels on the same tiling (two x columns per thread): stencil
 // codes + pore count, the MIXED x64 = x0 initialisation, and the tau flux.
 // ===========================================================================
@@ -232,7 +368,8 @@ __global__ void __launch_bounds__(NTHREADS) code_kernel(Launch L)
 }
 
 // MIXED: x64[0] = x0 (the reference's initial guess; its precision does not
-// matter to the converged iterate, so it is formed in FP32), e = 0.
+// matter to the converged iterate, so it is formed in FP32), e = 0 (and the
+// two-sweep BiCGSTAB vectors r, p, v, t = 0).
 __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
 {
     __shared__ int s_job;
@@ -244,12 +381,21 @@ __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
     const Geo g{J.nx, J.ny, J.nz, J.dir >> 1, (J.dir & 1) ? -1 : 1, J.pitch};
     double *x64 = J.x64[0];
     float *e = (float *)J.x;
+    // Two-sweep BiCGSTAB: the first replacement reads r, p, v (scaled by
+    // alpha = omega = 0) and step 1 reads t; all start at zero.
+    float *zr = (float *)J.r[0], *zp = (float *)J.p[0], *zv = (float *)J.v[0], *zt = (float *)J.t;
     for (int k = 0; k < 2; k++) {
         if (!t.v[k]) continue;
         for (int z = t.z0; z < t.z1; ++z) {
             const int64_t i = g.idx(t.gx + k, t.gy, z);
             x64[i] = (double)x0_at<float>(g, t.gx + k, t.gy, z);
             e[i] = 0.f;
+            if (zt) {
+                zr[i] = 0.f;
+                zp[i] = 0.f;
+                zv[i] = 0.f;
+                zt[i] = 0.f;
+            }
         }
     }
 }

@@ -1092,4 +1092,222 @@ struct OpBi3 {
     }
 };
 
+// ===========================================================================
+// MIXED BiCGSTAB in two sweeps per iteration (FP32 vectors, FP64 scalars).
+// The reference's three steps (BICGSTAB.cu:112-212) regroup so that every
+// global dot product still precedes the vectors that need it:
+//   step 1 (iteration k): r_k = s - w t and e += a y + w z of iteration k-1
+//     (pointwise, from r, v, t, p of k-1), then p_k = r_k + b (p - w v),
+//     v_k = A (p_k / diag); dots r0.v_k, |r_k|^2, r0.r_k;
+//   step 2: s = r_k - a v_k, t = A (s / diag) (stored); dots t.s, t.t, r0.t,
+//     r0.s, from which w = t.s / t.t and rho_{k+1} = r0.r_{k+1} =
+//     r0.s - w r0.t follow without a third sweep.
+// The FP64 residual replacement runs at the head of an iteration: it forms
+// the iterate of the pending updates on the fly, folds it into x64 and hands
+// fp32(b - A x64) to step 1 through t (k1_mode = 1: r_k = t, e = 0).
+// ===========================================================================
+__device__ __forceinline__ void bicg2_k1_finish(Scalars &sc, double r0v, double rr)
+{
+    sc.k1_mode = 0;
+    sc.rsq = rr;
+    sc.iter += 1;
+    if (!(rr <= sc.div_thresh)) {  // non-finite or exploding: restart from the true residual
+        sc.restarts += 1;
+        sc.replace = 2;
+        return;
+    }
+    sc.alpha = sc.rho / r0v;
+    if (!(fabs(sc.alpha) < 1e300)) {
+        sc.restarts += 1;
+        sc.replace = 2;
+        return;
+    }
+    mixed_request(sc, rr);
+}
+
+__device__ __forceinline__ void bicg2_k2_finish(Scalars &sc, double ts, double tt, double r0t, double r0s)
+{
+    const double omega = tt > 0.0 ? ts / tt : 0.0;
+    sc.omega = omega;
+    const double rho_new = r0s - omega * r0t;
+    const double rho_old = sc.rho;
+    sc.rho_old = rho_old;
+    sc.rho = rho_new;
+    // w = 0 (t vanished) or a shadow residual numerically orthogonal to r
+    // (in FP32, r0.r is noise well before |rho| reaches eps^2 |r0|^2): restart
+    // from the true residual.
+    if (omega == 0.0 || fabs(rho_new) < sc.eps2 * sc.r0_sq || rho_new * rho_new < sc.cos2_min * sc.r0_sq * sc.rsq) {
+        sc.restarts += 1;
+        sc.replace = 2;
+        return;
+    }
+    sc.beta = (rho_new / rho_old) * (sc.alpha / omega);
+}
+
+struct OpBiK1 {
+    using T = float;
+    static constexpr bool FB = true;
+    using SL = Streams<4, 4, 4, 4, 4, 4, 1>;  // r, v, t, p, e, r0, code
+    static constexpr int NV = 2;
+    using Shared = NoShared;
+    struct Vals { float r, v, t, p, e, r0; uint32_t code; };
+    struct Own { uint32_t code; float rk, pk, e, r0; };
+    struct Out { float r, p, v, e; };
+    const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
+    float *rnew, *pnew, *vnew, *e;
+    float cr, cv, ct, ce, beta, nomega, alpha, omega;
+    Acc<float> r0v, rr;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<float, SL, 0>(st, p, a.r, b.r);
+        sv2<float, SL, 1>(st, p, a.v, b.v);
+        sv2<float, SL, 2>(st, p, a.t, b.t);
+        sv2<float, SL, 3>(st, p, a.p, b.p);
+        sv2<float, SL, 4>(st, p, a.e, b.e);
+        sv2<float, SL, 5>(st, p, a.r0, b.r0);
+        load_code2<SL, 6>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a)
+    {
+        a.r = sv<float, SL, 0>(st, p);
+        a.v = sv<float, SL, 1>(st, p);
+        a.t = sv<float, SL, 2>(st, p);
+        a.p = sv<float, SL, 3>(st, p);
+        a.code = sv<uint8_t, SL, 6>(st, p);
+    }
+    __device__ void init(const Job &J, Shared &)
+    {
+        F = faces_of<T>(J);
+        const Scalars &sc = *J.sc;
+        const int par = (int)(sc.iter & 1);
+        tmap[0] = &J.tm[TM_R + par];
+        tmap[1] = &J.tm[TM_V + par];
+        tmap[2] = &J.tm[TM_T];
+        tmap[3] = &J.tm[TM_P + par];
+        tmap[4] = &J.tm[TM_X];
+        tmap[5] = &J.tm[TM_R0];
+        tmap[6] = &J.tm[TM_CODE];
+        rnew = (float *)J.r[par ^ 1];
+        pnew = (float *)J.p[par ^ 1];
+        vnew = (float *)J.v[par ^ 1];
+        e = (float *)J.x;
+        alpha = (float)sc.alpha;
+        omega = (float)sc.omega;
+        if (sc.k1_mode) {  // r_k = t (the true residual), e folded into x64
+            cr = 0.f; cv = 0.f; ct = 1.f; ce = 0.f;
+        } else {           // r_k = r - a v - w t
+            cr = 1.f; cv = -alpha; ct = -omega; ce = 1.f;
+        }
+        beta = (float)sc.beta;
+        nomega = -omega;
+    }
+    __device__ __forceinline__ float rk(const Vals &v) const { return cr * v.r + cv * v.v + ct * v.t; }
+    __device__ __forceinline__ float pk(const Vals &v, float r) const { return r + beta * (v.p + nomega * v.v); }
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps) const
+    {
+        return pk(v, rk(v)) * inv_of<T, FB>(C, g, v.code, ps);
+    }
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps, T &f) const
+    {
+        const float inv = inv_of<T, FB>(C, g, v.code, ps);
+        const float r = rk(v), p = pk(v, r);
+        f = p * inv;
+        // e_k = e + a y + w z, y = p_{k-1}/diag, z = s_{k-1}/diag
+        const float en = ce * (v.e + alpha * (v.p * inv) + omega * ((v.r - alpha * v.v) * inv));
+        return Own{v.code, r, p, en, v.r0};
+    }
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc, T fxp, T fxm,
+                         T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T vn = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        r0v.add_prod(o.r0, vn);
+        rr.add_prod(o.rk, o.rk);
+        return Out{o.rk, o.pk, vn, o.e};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0, bool v1)
+    {
+        store2<float>(rnew, i, a.r, b.r, v0, v1);
+        store2<float>(pnew, i, a.p, b.p, v0, v1);
+        store2<float>(vnew, i, a.v, b.v, v0, v1);
+        store2<float>(e, i, a.e, b.e, v0, v1);
+    }
+    __device__ void partials(T (&v_)[NV]) const { v_[0] = r0v.hi(); v_[1] = rr.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV]) { bicg2_k1_finish(sc, t[0], t[1]); }
+};
+
+struct OpBiK2 {
+    using T = float;
+    static constexpr bool FB = true;
+    using SL = Streams<4, 4, 4, 1>;  // r, v, r0, code
+    static constexpr int NV = 4;
+    using Shared = NoShared;
+    struct Vals { float r, v, r0; uint32_t code; };
+    struct Own { uint32_t code; float s, r0; };
+    struct Out { float t; };
+    const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
+    float *tout;
+    float nalpha;
+    Acc<float> ts, tt, r0t, r0s;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<float, SL, 0>(st, p, a.r, b.r);
+        sv2<float, SL, 1>(st, p, a.v, b.v);
+        sv2<float, SL, 2>(st, p, a.r0, b.r0);
+        load_code2<SL, 3>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a)
+    {
+        a.r = sv<float, SL, 0>(st, p);
+        a.v = sv<float, SL, 1>(st, p);
+        a.code = sv<uint8_t, SL, 3>(st, p);
+    }
+    __device__ void init(const Job &J, Shared &)
+    {
+        F = faces_of<T>(J);
+        const int par = (int)(J.sc->iter & 1);  // step 1 has counted the iteration
+        tmap[0] = &J.tm[TM_R + par];
+        tmap[1] = &J.tm[TM_V + par];
+        tmap[2] = &J.tm[TM_R0];
+        tmap[3] = &J.tm[TM_CODE];
+        tout = (float *)J.t;
+        nalpha = (float)(-J.sc->alpha);
+    }
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps) const
+    {
+        return (v.r + nalpha * v.v) * inv_of<T, FB>(C, g, v.code, ps);
+    }
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps, T &f) const
+    {
+        const float s = v.r + nalpha * v.v;
+        f = s * inv_of<T, FB>(C, g, v.code, ps);
+        return Own{v.code, s, v.r0};
+    }
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc, T fxp, T fxm,
+                         T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T t = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        ts.add_prod(t, o.s);
+        tt.add_prod(t, t);
+        r0t.add_prod(o.r0, t);
+        r0s.add_prod(o.r0, o.s);
+        return Out{t};
+    }
+    __device__ void store(int64_t i, const Out &a, const Out &b, bool v0, bool v1)
+    {
+        store2<float>(tout, i, a.t, b.t, v0, v1);
+    }
+    __device__ void partials(T (&v_)[NV]) const { v_[0] = ts.hi(); v_[1] = tt.hi(); v_[2] = r0t.hi(); v_[3] = r0s.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV]) { bicg2_k2_finish(sc, t[0], t[1], t[2], t[3]); }
+};
+
 }  // namespace ft

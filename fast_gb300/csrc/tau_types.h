@@ -36,7 +36,7 @@ enum SolveState : int32_t {
 // Tensor maps of a job's arrays (TMA descriptors), by array.
 enum TensorMapId : int {
     TM_CODE = 0, TM_X = 1, TM_R = 2 /* +parity */, TM_R0 = 4, TM_P = 5 /* +parity */, TM_V = 7 /* +parity */,
-    TM_X64 = 9 /* +parity */, NTM = 11
+    TM_X64 = 9 /* +parity */, TM_T = 11, NTM = 12
 };
 
 // Per right-hand-side solver scalars, resident in device memory and updated
@@ -72,7 +72,7 @@ struct Scalars {
     int32_t outer_steps;    // residual replacements done
     int32_t x64_cur;        // which x64 buffer holds the current iterate
     int32_t inner_mode;     // 1: MIXED solve
-    int32_t pad1;
+    int32_t k1_mode;        // two-sweep BiCGSTAB: 1 = the next step 1 takes r from t (just replaced), e = 0
     // reductions for tau and porosity
     double flux_sum;    // sum over voxels of the tau flux term
     uint64_t pores;     // number of zero (pore) voxels
@@ -98,6 +98,7 @@ struct Job {
     void *r0;                    // BiCGSTAB shadow residual (T)
     void *p[2];                  // search direction ping-pong (T)
     void *v[2];                  // BiCGSTAB v ping-pong (T)
+    void *t;                     // MIXED BiCGSTAB: t = A s, kept from step 2 to step 1 (FP32)
     double *x64[2];              // MIXED FP64 solution ping-pong
     Scalars *sc;
     double *part;                // ntiles * NPART partial sums
