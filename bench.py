@@ -46,13 +46,15 @@ import numpy as np  # noqa: E402
 WORKLOAD = dict(name="ellipsoids256_xyz_bicgstab_mixed", shape=(256, 256, 256), seed=1, semi_major=12.0,
                 aspect=0.35, solid_fraction=0.55, dirs=(0, 2, 4), tol=1e-7, max_iter=10000)
 
-# Compulsory bytes per voxel of each kernel of the FP32 BiCGSTAB step (each
-# stream the kernel touches read or written once; neighbour re-reads served
-# on chip).  Step 1 reads r, p, v, r0, code and writes p, v; step 2 reads r,
-# v, code; step 3 reads r, v, p, x, r0, code and writes x, r.  The FP64
-# residual replacement reads x64, e, code, r0 and writes x64, r.
-KERNEL_BYTES_PER_VOXEL = {"bi1": 25, "bi2": 9, "bi3": 29, "bi_restart": 13, "replace": 29, "tau": 9,
-                          "init64": 12, "code": 2, "cg1": 13, "cg2": 21}
+# Compulsory bytes per voxel of each kernel (each stream the kernel touches
+# read or written once; neighbour re-reads served on chip).  MIXED BiCGSTAB
+# runs two sweeps per iteration: step 1 ("bi1") reads r, v, t, p, e, r0, code
+# and writes r, p, v, e (41 B); step 2 ("bi2") reads r, v, r0, code and
+# writes t (17 B).  The FP64 residual replacement reads x64, e, p, r, v, r0,
+# code and writes x64, t (41 B).  CG: step 1 reads r, p, code, writes p;
+# step 2 reads p, x, r, code, writes x, r.
+KERNEL_BYTES_PER_VOXEL = {"bi1": 41, "bi2": 17, "replace": 41, "tau": 9, "init64": 12, "code": 2, "cg1": 13,
+                          "cg2": 21}
 # Algorithmic bytes per voxel-iteration of a whole FP32 BiCGSTAB iteration:
 # x, r, p, v read+written (32), r0 read (4), phase read twice (2).
 ITER_BYTES_FP32_BICGSTAB = 38
@@ -295,14 +297,14 @@ def run_ours(args, ws, rank, local):
     total_inner = sum(r.iterations for r in pres)
     kern = prof["kernels"]
     # voxels processed by all launches of a kernel kind
-    vox = {"bi1": N * total_inner, "bi2": N * total_inner, "bi3": N * total_inner,
+    vox = {"bi1": N * total_inner, "bi2": N * total_inner,
            "replace": N * sum(r.outer_steps for r in pres), "tau": N * len(dirs), "code": N,
            "init64": N * len(dirs)}
     dom = max(kern, key=lambda k: kern[k]["ms"])
     dom_bytes = KERNEL_BYTES_PER_VOXEL.get(dom, 0) * vox.get(dom, 0)
     dom_ms = kern[dom]["ms"]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
-    iter_ms = sum(kern.get(k, {"ms": 0})["ms"] for k in ("bi_restart", "bi1", "bi2", "bi3", "replace"))
+    iter_ms = sum(kern.get(k, {"ms": 0})["ms"] for k in ("bi1", "bi2", "replace"))
     iter_gbs = ITER_BYTES_FP32_BICGSTAB * N * total_inner / (iter_ms / 1e3) / 1e9 if iter_ms > 0 else 0.0
     launches_per_step = launches / max(args.steps, 1)
 
@@ -383,9 +385,9 @@ def run_ours(args, ws, rank, local):
 C_RESULT_BYTES = 40  # sizeof(fast_tau_result)
 # DRAM bytes (read + write) per bench launch of each kernel, from one ncu
 # --set full capture of a one-direction launch of the same volume
-# (profiles/bi1_bi3_ellipsoids256_x_full.md), scaled by 3 to the three
-# right-hand sides a bench launch processes (traffic grows with the voxels).
-NCU_TRAFFIC = {"bi1": 3 * 415.2e6, "bi3": 3 * 518.7e6}
+# (profiles/), scaled by 3 to the three right-hand sides a bench launch
+# processes (traffic grows with the voxels).  Empty until captured.
+NCU_TRAFFIC = {}
 
 
 # ---------------------------------------------------------------------------
@@ -680,15 +682,17 @@ def run_c5(args):
 
 def run_ncu_case(args):
     """A short, fixed run of the workload's kernels for profiler captures:
-    the bench volume, one direction (x), MIXED BiCGSTAB stopped after
-    --ncu-iters iterations.  Prints the iteration count; times nothing."""
+    the bench volume, one direction (x), MIXED BiCGSTAB (or CG with
+    --ncu-solver cg) stopped after --ncu-iters iterations.  Prints the
+    iteration count; times nothing."""
     import torch
     import fast_gb300 as ft
     w = WORKLOAD
     mask = make_volume()
     d_mask = torch.from_numpy(mask).cuda()
     p = ft.TortuosityParams(tolerance=1e-12, max_iter=args.ncu_iters, precision=ft.Precision.MIXED)
-    res = ft.solve_directions_device(d_mask.data_ptr(), mask.shape, [ft.Dir.X_POS], p, ft.DSOLVER_BICGSTAB)
+    solver = ft.DSOLVER_CG if args.ncu_solver == "cg" else ft.DSOLVER_BICGSTAB
+    res = ft.solve_directions_device(d_mask.data_ptr(), mask.shape, [ft.Dir.X_POS], p, solver)
     torch.cuda.synchronize()
     print(json.dumps({"ncu_case": w["name"] + "_x", "iterations": res[0].iterations, "status": int(res[0].status)}))
 
@@ -704,6 +708,7 @@ def main():
     ap.add_argument("--ncu-case", action="store_true",
                     help="run a short fixed slice of the workload for profiler captures and exit")
     ap.add_argument("--ncu-iters", type=int, default=12)
+    ap.add_argument("--ncu-solver", default="bicgstab", choices=["bicgstab", "cg"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default) is the headline; the others print their own line")
     ap.add_argument("--requests", type=int, default=64, help="c4: requests in the stream")

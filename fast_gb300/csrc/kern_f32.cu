@@ -11,18 +11,24 @@ namespace ft {
 // Depth of the TMA stage ring (planes of every operand in flight per block).
 constexpr int kStages = FAST_TAU_STAGES_F32;
 
-template <class Op>
+#ifndef FAST_TAU_STAGES_K1
+#define FAST_TAU_STAGES_K1 4
+#endif
+// Stage ring of the two-sweep BiCGSTAB step 1 (seven streams per plane).
+constexpr int kStagesK1 = FAST_TAU_STAGES_K1;
+
+template <class Op, int NS = kStages>
 static void go(const Launch &L, cudaStream_t st)
 {
-    constexpr int dyn = sweep_dyn_smem<Op, kStages>();
-    sweep_kernel<Op, kStages><<<(unsigned)L.nblocks, NTHREADS, dyn, st>>>(L);
+    constexpr int dyn = sweep_dyn_smem<Op, NS>();
+    sweep_kernel<Op, NS><<<(unsigned)L.nblocks, NTHREADS, dyn, st>>>(L);
 }
 
-template <class Op>
+template <class Op, int NS = kStages>
 static cudaError_t cfg()
 {
-    return cudaFuncSetAttribute(sweep_kernel<Op, kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                sweep_dyn_smem<Op, kStages>());
+    return cudaFuncSetAttribute(sweep_kernel<Op, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                sweep_dyn_smem<Op, NS>());
 }
 
 template <typename ST>
@@ -61,7 +67,7 @@ static cudaError_t configure()
 cudaError_t configure_f32()
 {
     cudaError_t a = configure<float>(), b = configure<double>();
-    cudaError_t c = cfg<OpBiK1>(), d = cfg<OpBiK2>();
+    cudaError_t c = cfg<OpBiK1, kStagesK1>(), d = cfg<OpBiK2>();
     if (a != cudaSuccess) return a;
     if (b != cudaSuccess) return b;
     return c != cudaSuccess ? c : d;
@@ -70,7 +76,7 @@ cudaError_t configure_f32()
 void launch_pure_f32(Step s, const Launch &L, cudaStream_t st) { dispatch<float>(s, L, st); }
 void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st)
 {
-    if (s == Step::BI_K1) go<OpBiK1>(L, st);
+    if (s == Step::BI_K1) go<OpBiK1, kStagesK1>(L, st);
     else if (s == Step::BI_K2) go<OpBiK2>(L, st);
     else dispatch<double>(s, L, st);
 }

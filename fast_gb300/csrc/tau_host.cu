@@ -524,9 +524,9 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     S.tol_outer = P.tolerance;
     // MIXED: the first step is a replacement with restart (x64 = x0, e = 0).
     S.replace = mixed ? 2 : 0;
-    const double delta = env_double("FAST_TAU_REPLACE_DELTA", 0.1);
+    const double delta = env_double("FAST_TAU_REPLACE_DELTA", 0.03);
     S.delta2 = delta * delta;
-    const double cmin = env_double("FAST_TAU_SHADOW_COS", 1e-4);
+    const double cmin = env_double("FAST_TAU_SHADOW_COS", 1e-6);
     S.cos2_min = cmin * cmin;
     S.inner_mode = mixed ? 1 : 0;
     // MIXED BiCGSTAB: no update is pending before the first replacement.
