@@ -19,7 +19,9 @@
 // iterating while the host retires and admits.  Chunks carry sequence
 // numbers; a snapshot speaks only for solves admitted before its chunk.  All
 // work is on one stream, so a slot or job table reused for a new solve is
-// rewritten only after every queued chunk that names its previous owner.
+// rewritten only after every queued chunk that names its previous owner; the
+// host-side staging of those copies is rewritten only after the previous
+// step's copies out of it have run.
 // A request's arithmetic is exactly that of a solve of it alone: its kernels
 // see only its own scalars and partial sums, whatever else shares the
 // launches.  There is no counterpart in the reference (fast tau solves one
@@ -95,6 +97,11 @@ struct Ctx {
     int inflight = 0, head = 0;
     cudaEvent_t ev[2] = {};
     uint64_t snap_seq[2] = {};
+    // Recorded behind a step's copies out of the pinned staging (new solves'
+    // scalars, job tables); the next step waits for it before rewriting the
+    // staging, since the chunk it consumes may precede those copies.
+    cudaEvent_t ev_copy = nullptr;
+    bool copy_pending = false;
     uint64_t next_seq = 0;
     uint64_t next_ticket = 1;
     size_t bytes_inflight = 0;
@@ -344,6 +351,10 @@ int step(Ctx &C, fast_ctx_completion *out, int32_t cap, int32_t *n_out)
         int s = launch_chunk(C);
         if (s != FAST_OK) return s;
     }
+    if (C.copy_pending) {
+        SV(cudaEventSynchronize(C.ev_copy));
+        C.copy_pending = false;
+    }
     if (C.inflight > 0) {
         const int b = C.head;
         SV(cudaEventSynchronize(C.ev[b]));
@@ -359,6 +370,8 @@ int step(Ctx &C, fast_ctx_completion *out, int32_t cap, int32_t *n_out)
         s = rebuild(C);
         if (s != FAST_OK) return s;
     }
+    SV(cudaEventRecord(C.ev_copy, C.st));
+    C.copy_pending = true;
     while (C.inflight < 2) {
         s = launch_chunk(C);
         if (s != FAST_OK) return s;
@@ -386,6 +399,7 @@ void destroy(Ctx *C)
     if (C->h_stage) cudaFreeHost(C->h_stage);
     for (cudaEvent_t e : C->ev)
         if (e) cudaEventDestroy(e);
+    if (C->ev_copy) cudaEventDestroy(C->ev_copy);
     if (C->st) cudaStreamDestroy(C->st);
     delete C;
 }
@@ -421,7 +435,8 @@ int create(const fast_ctx_config &cfg, Ctx **out)
     };
     if (cudaStreamCreateWithFlags(&C->st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&C->ev[0], cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&C->ev[1], cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&C->ev[1], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&C->ev_copy, cudaEventDisableTiming) != cudaSuccess)
         return fin(ft_fail(FAST_CUDA_ERROR, "stream/event creation failed"));
     if (cudaMallocAsync((void **)&C->d_slots, sizeof(Scalars) * K, C->st) != cudaSuccess ||
         cudaMallocAsync((void **)&C->d_cnt, sizeof(uint32_t) * K, C->st) != cudaSuccess ||
