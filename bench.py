@@ -386,8 +386,8 @@ C_RESULT_BYTES = 40  # sizeof(fast_tau_result)
 # DRAM bytes (read + write) per bench launch of each kernel, from one ncu
 # --set full capture of a one-direction launch of the same volume
 # (profiles/), scaled by 3 to the three right-hand sides a bench launch
-# processes (traffic grows with the voxels).  Empty until captured.
-NCU_TRAFFIC = {}
+# processes (traffic grows with the voxels).
+NCU_TRAFFIC = {"bi1": 3 * 665.8e6, "bi2": 3 * 275.4e6}
 
 
 # ---------------------------------------------------------------------------
