@@ -18,9 +18,11 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfasttau.so")
+CLI = os.path.join(OUT, "fast")  # the `fast tau` command-line drop-in
 
 CUDA_SOURCES = ["kern_f64.cu", "kern_f32.cu", "kern_misc.cu", "tau_host.cu", "noalloc.cu", "ccl.cu", "serve.cu"]
 CXX_SOURCES = ["gen.cpp"]
+CLI_SOURCE = "fast_cli.cpp"
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -32,16 +34,16 @@ def _nvcc() -> str:
 
 
 def _inputs():
-    files = [os.path.join(CSRC, f) for f in CUDA_SOURCES + CXX_SOURCES]
+    files = [os.path.join(CSRC, f) for f in CUDA_SOURCES + CXX_SOURCES + [CLI_SOURCE]]
     files += glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
     files += glob.glob(os.path.join(INCLUDE, "*.h"))
     return files
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
     return all(os.path.getmtime(f) <= t for f in _inputs())
 
 
@@ -79,6 +81,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
     os.replace(tmp, LIB)
+    # The CLI links the library from its own directory.
+    tmp = CLI + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-I", INCLUDE, os.path.join(CSRC, CLI_SOURCE), "-o", tmp,
+           "-L", OUT, "-lfasttau", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode:
+        raise RuntimeError("CLI build failed:\n" + r.stdout.decode(errors="replace"))
+    os.replace(tmp, CLI)
     return LIB
 
 

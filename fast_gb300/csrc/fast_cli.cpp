@@ -1,0 +1,334 @@
+// `fast tau`: the command-line drop-in for the reference's tortuosity action
+// (fast/src/main.cpp, fast/src/TauModule.h:14-153, VolumeIOModule.h:139-253,
+// CSVOutputModule.h:35-112), over libfasttau.so's C ABI.
+//
+//   fast tau <input.bin> [-d x|y|z|xy..|all|pos|neg|xneg|yneg|zneg]
+//            [--solver CG|BICGSTAB] [--tol N] [--iter N] [-p d|f|mixed]
+//            [--sub x[,y,z]] [--origin x[,y,z]] [--randsub x[,y,z]]
+//            [--aspect x,y,z] [-o out.csv] [-v] [--cpu] [-j N] [--over]
+//
+// For every direction one row is written (stdout, or appended to -o; the
+// header goes first when the file is new), with the reference's columns in
+// its order (a std::map of column names, so sorted): ID, device, dimx, dimy,
+// dimz, dir, porosity, precision, tau, tauIter, tauNU, tauSolver, tauTime,
+// tauTolerance.  As in the reference the porosity is computed once per
+// volume, rounded to float and passed to every direction as precomputed, and
+// tauTime covers one direction's getTortuosity call.  Every solve runs on the
+// GPU: --cpu and -j are accepted for compatibility and change nothing
+// (device is reported as GPU); --over has no counterpart.  -p mixed selects
+// the engine's mixed-precision solver (precision column "mixed").  Input is a
+// .bin volume (VolumeIO.cpp:279-305: int32 PrimitiveType, int32 x 3
+// dimensions, one bool byte, raw x-fastest data) of type uchar; TIFF folders,
+// .sph and .pos inputs are not read.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <random>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "fasttau.h"
+
+namespace {
+
+constexpr int32_t kTypeUchar = 2;  // PrimitiveType TYPE_UCHAR (PrimitiveTypes.h:11-24)
+
+struct Vol {
+    int64_t nx = 0, ny = 0, nz = 0;
+    std::vector<uint8_t> data;  // x fastest
+};
+
+int usage(const char *why)
+{
+    if (why) std::cerr << "error: " << why << "\n";
+    std::cerr << "usage: fast tau <input.bin> [-d x|y|z|all|pos|neg] [--solver CG|BICGSTAB] [--tol N]\n"
+                 "                [--iter N] [-p d|f|mixed] [--sub x,y,z] [--origin x,y,z] [--randsub x,y,z]\n"
+                 "                [--aspect x,y,z] [-o out.csv] [-v] [--cpu] [-j N]\n";
+    return why ? 1 : 0;
+}
+
+bool ends_with(const std::string &s, const std::string &ext)
+{
+    const size_t d = s.find_last_of('.');
+    return d != std::string::npos && s.substr(d + 1) == ext;
+}
+
+// "x" or "x,y,z" (IVec3Reader / Vec3Reader, fast/src/utility.h:34-66).
+template <typename T>
+bool parse3(const std::string &v, T out[3])
+{
+    std::stringstream ss(v);
+    std::string item;
+    std::vector<std::string> parts;
+    while (std::getline(ss, item, ',')) parts.push_back(item);
+    try {
+        if (parts.size() == 1) {
+            out[0] = out[1] = out[2] = (T)std::stod(parts[0]);
+        } else if (parts.size() == 3) {
+            for (int k = 0; k < 3; k++) out[k] = (T)std::stod(parts[k]);
+        } else {
+            return false;
+        }
+    } catch (...) {
+        return false;
+    }
+    return true;
+}
+
+// getDirs (fast/src/utility.h:77-109).
+std::vector<int32_t> get_dirs(const std::string &f)
+{
+    if (f == "all") return {FAST_X_POS, FAST_X_NEG, FAST_Y_POS, FAST_Y_NEG, FAST_Z_POS, FAST_Z_NEG};
+    if (f == "pos") return {FAST_X_POS, FAST_Y_POS, FAST_Z_POS};
+    if (f == "neg") return {FAST_X_NEG, FAST_Y_NEG, FAST_Z_NEG};
+    if (f == "xneg") return {FAST_X_NEG};
+    if (f == "yneg") return {FAST_Y_NEG};
+    if (f == "zneg") return {FAST_Z_NEG};
+    std::vector<int32_t> d;
+    for (char c : f) {
+        if (c == 'x') d.push_back(FAST_X_POS);
+        else if (c == 'y') d.push_back(FAST_Y_POS);
+        else if (c == 'z') d.push_back(FAST_Z_POS);
+    }
+    if (d.empty()) d.push_back(FAST_X_POS);
+    return d;
+}
+
+const char *dir_string(int32_t d)
+{
+    static const char *names[] = {"X_POS", "X_NEG", "Y_POS", "Y_NEG", "Z_POS", "Z_NEG"};
+    return (d >= 0 && d < 6) ? names[d] : "DIR_NONE";
+}
+
+// loadVolumeBinary (fastlib/src/volume/VolumeIO.cpp:279-305).
+bool load_bin(const std::string &path, Vol &v, std::string &err)
+{
+    std::ifstream f(path, std::ios::binary);
+    if (!f.good()) {
+        err = "Couldn't read file";
+        return false;
+    }
+    int32_t type = 0, dim[3] = {0, 0, 0};
+    char flag = 0;
+    f.read((char *)&type, 4);
+    f.read((char *)dim, 12);
+    f.read(&flag, 1);
+    if (!f.good()) {
+        err = "truncated header";
+        return false;
+    }
+    if (type != kTypeUchar) {
+        err = "Mask must by type uchar";  // VolumeMeasures.cpp:50
+        return false;
+    }
+    if (dim[0] <= 0 || dim[1] <= 0 || dim[2] <= 0) {
+        err = "bad dimensions";
+        return false;
+    }
+    v.nx = dim[0];
+    v.ny = dim[1];
+    v.nz = dim[2];
+    v.data.resize((size_t)(v.nx * v.ny * v.nz));
+    f.read((char *)v.data.data(), (std::streamsize)v.data.size());
+    if ((size_t)f.gcount() != v.data.size()) {
+        err = "truncated data";
+        return false;
+    }
+    return true;
+}
+
+// Volume::resize(origin, size): keep the box [origin, origin + size).
+Vol crop(const Vol &v, const int64_t o[3], const int64_t s[3])
+{
+    Vol r;
+    r.nx = s[0];
+    r.ny = s[1];
+    r.nz = s[2];
+    r.data.resize((size_t)(r.nx * r.ny * r.nz));
+    for (int64_t z = 0; z < r.nz; z++)
+        for (int64_t y = 0; y < r.ny; y++)
+            memcpy(&r.data[(size_t)(r.nx * (y + r.ny * z))],
+                   &v.data[(size_t)(o[0] + v.nx * (o[1] + y + v.ny * (o[2] + z)))], (size_t)r.nx);
+    return r;
+}
+
+struct Row {
+    std::string id, dir, precision, solver;
+    int64_t dim[3];
+    double porosity, tau, time, tol;
+    int iter;
+};
+
+// CSVOutputModule::addRunRow (CSVOutputModule.h:35-89): header when the
+// output is new (file absent, or the first row to stdout), appended rows.
+void write_row(const std::string &out_path, bool &first_stdout, const Row &r)
+{
+    std::ostringstream line;
+    line << r.id << "," << "GPU" << "," << r.dim[0] << "," << r.dim[1] << "," << r.dim[2] << "," << r.dir << ","
+         << r.porosity << "," << r.precision << "," << r.tau << "," << r.iter << "," << 0 << "," << r.solver << ","
+         << r.time << "," << r.tol << "\n";
+    const char *header = "ID,device,dimx,dimy,dimz,dir,porosity,precision,tau,tauIter,tauNU,tauSolver,tauTime,"
+                         "tauTolerance\n";
+    if (out_path.empty()) {
+        if (first_stdout) std::cout << header;
+        first_stdout = false;
+        std::cout << line.str();
+        std::cout.flush();
+        return;
+    }
+    bool is_new;
+    {
+        std::ifstream f(out_path);
+        is_new = !f.is_open();
+    }
+    std::ofstream f(out_path, std::ios::app);
+    if (is_new) f << header;
+    f << line.str();
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    if (argc < 2) return usage("missing action");
+    const std::string action = argv[1];
+    if (action == "-h" || action == "--help") return usage(nullptr);
+    if (action != "tau") return usage("only the `tau` action is built");
+
+    std::string input, dir = "x-", solver = "CG", precision = "double", out_path;
+    int tol_exp = 6;
+    long long max_iter = 10000;
+    bool verbose = false, has_sub = false, has_origin = false, has_rand = false, has_aspect = false;
+    int64_t sub[3] = {0, 0, 0}, origin[3] = {0, 0, 0}, randsub[3] = {0, 0, 0};
+    float aspect[3] = {1.f, 1.f, 1.f};
+    for (int i = 2; i < argc; i++) {
+        const std::string a = argv[i];
+        auto next = [&](const char *what) -> std::string {
+            if (i + 1 >= argc) {
+                std::cerr << "error: " << what << " needs a value\n";
+                std::exit(1);
+            }
+            return argv[++i];
+        };
+        if (a == "-h" || a == "--help") return usage(nullptr);
+        else if (a == "-d" || a == "--dir") dir = next("-d");
+        else if (a == "--solver") solver = next("--solver");
+        else if (a == "--tol") tol_exp = std::atoi(next("--tol").c_str());
+        else if (a == "--iter") max_iter = std::atoll(next("--iter").c_str());
+        else if (a == "-p" || a == "--precision") precision = next("-p");
+        else if (a == "-o" || a == "--output") out_path = next("-o");
+        else if (a == "-v" || a == "--verbose") verbose = true;
+        else if (a == "--cpu" || a == "--over" || a == "--oversubscribe") { /* accepted, no effect */ }
+        else if (a == "-j" || a == "--cputhreads") next("-j");
+        else if (a == "--sub") has_sub = parse3(next("--sub"), sub);
+        else if (a == "--origin") has_origin = parse3(next("--origin"), origin);
+        else if (a == "--randsub") has_rand = parse3(next("--randsub"), randsub);
+        else if (a == "--aspect") has_aspect = parse3(next("--aspect"), aspect);
+        else if (!a.empty() && a[0] == '-') return usage(("unknown option " + a).c_str());
+        else if (input.empty()) input = a;
+        else return usage("more than one input");
+    }
+    if (input.empty()) return usage("Invalid input");
+    if (!ends_with(input, "bin")) return usage("only .bin volume files are read");
+
+    Vol vol;
+    std::string err;
+    if (!load_bin(input, vol, err)) {
+        std::cerr << "Failed to load: " << err << "\n";
+        return 1;
+    }
+    // Crops (VolumeIOModule.h:180-248).
+    if (has_sub || (has_origin && (origin[0] || origin[1] || origin[2]))) {
+        const int64_t dim[3] = {vol.nx, vol.ny, vol.nz};
+        int64_t lo[3], hi[3], size[3];
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(std::max(origin[k], (int64_t)0), dim[k]);
+            hi[k] = std::min(std::max(origin[k] + sub[k], (int64_t)0), dim[k]);
+            if (hi[k] <= lo[k]) {
+                std::cerr << "error: Invalid resize options\n";
+                return 1;
+            }
+            size[k] = hi[k] - lo[k];
+        }
+        vol = crop(vol, lo, size);
+    } else if (has_rand) {
+        const int64_t dim[3] = {vol.nx, vol.ny, vol.nz};
+        std::mt19937_64 rng((uint64_t)std::chrono::system_clock::now().time_since_epoch().count());
+        int64_t lo[3];
+        for (int k = 0; k < 3; k++) {
+            const int64_t room = dim[k] - randsub[k];
+            if (randsub[k] <= 0 || room <= 0) {
+                std::cerr << "error: Invalid resize options\n";
+                return 1;
+            }
+            lo[k] = (int64_t)(rng() % (uint64_t)room);
+        }
+        vol = crop(vol, lo, randsub);
+    }
+    if (has_aspect) {
+        int k = aspect[0] == 1.f ? 0 : (aspect[1] == 1.f ? 1 : (aspect[2] == 1.f ? 2 : -1));
+        if (k < 0) {
+            std::cerr << "error: Invalid aspect options, one dimension must equal to 1.0\n";
+            return 1;
+        }
+        const int64_t dim[3] = {vol.nx, vol.ny, vol.nz};
+        int64_t size[3];
+        for (int a = 0; a < 3; a++) size[a] = std::min(std::max((int64_t)(dim[k] * aspect[a]), (int64_t)0), dim[a]);
+        const int64_t lo[3] = {0, 0, 0};
+        vol = crop(vol, lo, size);
+    }
+
+    fast_tau_params p;
+    fast_tau_params_init(&p);
+    p.solver = solver == "BICGSTAB" ? FAST_SOLVER_BICGSTAB : FAST_SOLVER_CG;
+    std::string prec_name = "double";
+    if (precision == "float" || precision == "single" || precision == "f" || precision == "s") {
+        p.precision = FAST_PREC_F32;
+        prec_name = "single";
+    } else if (precision == "mixed" || precision == "m") {
+        p.precision = FAST_PREC_MIXED;
+        prec_name = "mixed";
+    } else {
+        p.precision = FAST_PREC_F64;
+    }
+    p.tolerance = std::pow(10.0, -tol_exp);
+    p.max_iter = (uint64_t)max_iter;
+    p.verbose = verbose ? 1 : 0;
+
+    double phi = 0.0;
+    int st = fast_porosity(vol.data.data(), vol.nx, vol.ny, vol.nz, &phi, nullptr);
+    if (st != FAST_OK) {
+        std::cerr << "error: " << fast_last_error() << "\n";
+        return 1;
+    }
+    // TauModule.h:68,80-81: float porosity, passed as precomputed.
+    p.porosity = (double)(float)phi;
+
+    bool first_stdout = true;
+    int status = 0;
+    for (int32_t d : get_dirs(dir)) {
+        p.dir = d;
+        if (verbose) std::cout << "Tau Direction " << d << std::endl;
+        double tau = 0.0;
+        uint64_t iters = 0;
+        const auto t0 = std::chrono::system_clock::now();
+        st = fast_tau_solve(vol.data.data(), vol.nx, vol.ny, vol.nz, &p, &tau, &iters, nullptr, nullptr);
+        const std::chrono::duration<double> dt = std::chrono::system_clock::now() - t0;
+        if (st != FAST_OK) {
+            std::cerr << fast_last_error() << "\n";  // tau = 0, as the reference reports a failed solve
+            if (st == FAST_CUDA_ERROR || st == FAST_NOMEM || st == FAST_TIMEOUT || st == FAST_BAD_ARG) status = 1;
+        }
+        if (verbose) std::cout << "Elapsed: " << dt.count() << "s (" << dt.count() / 60.0 << "m)" << std::endl;
+        Row r{input, dir_string(d), prec_name, p.solver == FAST_SOLVER_BICGSTAB ? "BICGSTAB" : "CG",
+              {vol.nx, vol.ny, vol.nz}, p.porosity, tau, dt.count(), p.tolerance, (int)iters};
+        write_row(out_path, first_stdout, r);
+    }
+    return status;
+}
