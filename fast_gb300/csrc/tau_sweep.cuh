@@ -192,8 +192,9 @@ __host__ __device__ constexpr int sweep_dyn_smem()
 // holds x0 + TX.
 constexpr int PW = TX + 4;
 
+// The sweep body, shared by the kernel entries below.
 template <class Op, int NSTAGE>
-__global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
+__device__ __forceinline__ void sweep_body(const Launch &L)
 {
     using T = typename Op::T;
     using SL = typename Op::SL;
@@ -405,6 +406,20 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
             *J.counter = 0u;
         }
     }
+}
+
+// Kernel entries: the compiler's own register choice, or (for an operation
+// that is otherwise held to two blocks per SM) a bound that fits MB blocks.
+template <class Op, int NSTAGE>
+__global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
+{
+    sweep_body<Op, NSTAGE>(L);
+}
+
+template <class Op, int NSTAGE, int MB>
+__global__ void __launch_bounds__(NTHREADS, MB) sweep_kernel_mb(Launch L)
+{
+    sweep_body<Op, NSTAGE>(L);
 }
 
 // ---------------------------------------------------------------------------
