@@ -96,6 +96,11 @@ SIGNATURES = {
                                         C.POINTER(C.c_uint32), C.c_void_p, C.c_uint64, C.c_void_p]),
     "fast_ccl_boundary_device": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint32, C.c_void_p,
                                            C.c_void_p]),
+    "fast_tiff_folder_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_int64)]),
+    "fast_tiff_folder_read": (C.c_int, [C.c_char_p, C.c_void_p, C.c_uint64]),
+    "fast_binarize": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float]),
+    "fast_binarize_device": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float, C.c_void_p]),
     "fast_last_error": (C.c_char_p, []),
     "fast_version": (C.c_char_p, []),
     "fast_gen_spheres": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_double,

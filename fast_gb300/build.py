@@ -20,8 +20,9 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfasttau.so")
 CLI = os.path.join(OUT, "fast")  # the `fast tau` command-line drop-in
 
-CUDA_SOURCES = ["kern_f64.cu", "kern_f32.cu", "kern_misc.cu", "tau_host.cu", "noalloc.cu", "ccl.cu", "serve.cu"]
-CXX_SOURCES = ["gen.cpp"]
+CUDA_SOURCES = ["kern_f64.cu", "kern_f32.cu", "kern_misc.cu", "tau_host.cu", "noalloc.cu", "ccl.cu", "serve.cu",
+                "volume_ops.cu"]
+CXX_SOURCES = ["gen.cpp", "tiff_folder.cpp"]
 CLI_SOURCE = "fast_cli.cpp"
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -63,7 +64,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for src in CXX_SOURCES:
         obj = os.path.join(OUT, src.replace(".cpp", ".o"))
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off",
-               "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+               "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj]
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
         objs.append(obj)
     failed = []

@@ -2,7 +2,7 @@
 // (fast/src/main.cpp, fast/src/TauModule.h:14-153, VolumeIOModule.h:139-253,
 // CSVOutputModule.h:35-112), over libfasttau.so's C ABI.
 //
-//   fast tau <input.bin> [-d x|y|z|xy..|all|pos|neg|xneg|yneg|zneg]
+//   fast tau <input.bin|tiff folder> [-d x|y|z|xy..|all|pos|neg|xneg|yneg|zneg]
 //            [--solver CG|BICGSTAB] [--tol N] [--iter N] [-p d|f|mixed]
 //            [--sub x[,y,z]] [--origin x[,y,z]] [--randsub x[,y,z]]
 //            [--aspect x,y,z] [-o out.csv] [-v] [--cpu] [-j N] [--over]
@@ -18,8 +18,12 @@
 // (device is reported as GPU); --over has no counterpart.  -p mixed selects
 // the engine's mixed-precision solver (precision column "mixed").  Input is a
 // .bin volume (VolumeIO.cpp:279-305: int32 PrimitiveType, int32 x 3
-// dimensions, one bool byte, raw x-fastest data) of type uchar; TIFF folders,
-// .sph and .pos inputs are not read.
+// dimensions, one bool byte, raw x-fastest data) of type uchar, or a folder
+// of 8-bit TIFF slices, which is read (fast_tiff_folder_read) and binarized
+// with threshold 1.0 on the GPU (fast_binarize) as VolumeIOModule.h:57-63
+// does.  .sph and .pos inputs (particle rasterisation) are not read.
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -48,7 +52,7 @@ struct Vol {
 int usage(const char *why)
 {
     if (why) std::cerr << "error: " << why << "\n";
-    std::cerr << "usage: fast tau <input.bin> [-d x|y|z|all|pos|neg] [--solver CG|BICGSTAB] [--tol N]\n"
+    std::cerr << "usage: fast tau <input.bin|tiff folder> [-d x|y|z|all|pos|neg] [--solver CG|BICGSTAB] [--tol N]\n"
                  "                [--iter N] [-p d|f|mixed] [--sub x,y,z] [--origin x,y,z] [--randsub x,y,z]\n"
                  "                [--aspect x,y,z] [-o out.csv] [-v] [--cpu] [-j N]\n";
     return why ? 1 : 0;
@@ -105,6 +109,29 @@ const char *dir_string(int32_t d)
 {
     static const char *names[] = {"X_POS", "X_NEG", "Y_POS", "Y_NEG", "Z_POS", "Z_NEG"};
     return (d >= 0 && d < 6) ? names[d] : "DIR_NONE";
+}
+
+bool is_directory(const std::string &path)
+{
+    struct stat st;
+    return stat(path.c_str(), &st) == 0 && S_ISDIR(st.st_mode);
+}
+
+// loadTiffFolder + binarize(1.0) (VolumeIOModule.h:57-63): the slices' raw
+// values, then v < 255 -> 0, else 255, on the GPU.
+bool load_tiff_folder(const std::string &path, Vol &v, std::string &err)
+{
+    if (fast_tiff_folder_info(path.c_str(), &v.nx, &v.ny, &v.nz) != FAST_OK) {
+        err = fast_last_error();
+        return false;
+    }
+    v.data.resize((size_t)(v.nx * v.ny * v.nz));
+    if (fast_tiff_folder_read(path.c_str(), v.data.data(), v.data.size()) != FAST_OK ||
+        fast_binarize(v.data.data(), v.data.size(), 1.0f) != FAST_OK) {
+        err = fast_last_error();
+        return false;
+    }
+    return true;
 }
 
 // loadVolumeBinary (fastlib/src/volume/VolumeIO.cpp:279-305).
@@ -236,13 +263,21 @@ int main(int argc, char **argv)
         else return usage("more than one input");
     }
     if (input.empty()) return usage("Invalid input");
-    if (!ends_with(input, "bin")) return usage("only .bin volume files are read");
 
     Vol vol;
     std::string err;
-    if (!load_bin(input, vol, err)) {
-        std::cerr << "Failed to load: " << err << "\n";
-        return 1;
+    if (is_directory(input)) {
+        if (!load_tiff_folder(input, vol, err)) {
+            std::cerr << "Failed to load: " << err << "\n";
+            return 1;
+        }
+    } else if (ends_with(input, "bin")) {
+        if (!load_bin(input, vol, err)) {
+            std::cerr << "Failed to load: " << err << "\n";
+            return 1;
+        }
+    } else {
+        return usage("input must be a .bin volume or a folder of TIFF slices");
     }
     // Crops (VolumeIOModule.h:180-248).
     if (has_sub || (has_origin && (origin[0] || origin[1] || origin[2]))) {

@@ -79,6 +79,7 @@ class Status(IntEnum):
     CUDA_ERROR = 6
     TIMEOUT = 7
     BAD_ARG = 8
+    IO_ERROR = 9
 
 
 def _f32(v: float) -> float:
@@ -143,6 +144,17 @@ class Volume:
 
     def sum_zero_elems(self) -> int:
         return get_pore_count(self.data)
+
+    def binarize(self, threshold: float = 1.0) -> None:
+        """Volume::binarize (Volume.cpp:478-486): v < uchar(threshold*255)
+        -> 0, else 255, on the GPU (fast_binarize), in place."""
+        if self.type() != Volume.TYPE_UCHAR:
+            raise TypeError("binarize reads uint8 volumes")
+        arr = np.ascontiguousarray(self.data)
+        st = _native.lib().fast_binarize(arr.ctypes.data_as(C.c_void_p), arr.size, float(threshold))
+        if st != Status.OK:
+            raise RuntimeError(f"binarize failed ({Status(st).name}): {_native.last_error()}")
+        self.data = arr
 
 
 @dataclass

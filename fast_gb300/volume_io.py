@@ -3,9 +3,11 @@ VolumeIO.cpp:256-305 saveVolumeBinary / loadVolumeBinary): a 17-byte header
 -- int32 PrimitiveType, int32 x 3 dimensions (x, y, z), one bool byte the
 reference no longer uses -- then the raw voxels, x fastest, little endian.
 Arrays here are [z, y, x] (x fastest in memory), as everywhere in the
-package; the tortuosity path reads PrimitiveType UCHAR (2) volumes."""
+package; the tortuosity path reads PrimitiveType UCHAR (2) volumes.  Folders
+of TIFF slices (loadTiffFolder) are read by load_tiff_folder."""
 from __future__ import annotations
 
+import os
 import struct
 
 import numpy as np
@@ -69,4 +71,32 @@ def load_volume_binary(path: str):
     return Volume(arr) if code == Volume.TYPE_UCHAR else arr
 
 
-__all__ = ["load_volume_binary", "save_volume_binary", "PRIMITIVE_TYPES"]
+def load_tiff_folder(folder: str, binarize: bool = False, threshold: float = 1.0) -> Volume:
+    """loadTiffFolder (VolumeIO.cpp:197-254): the folder's *.tif / *.tiff
+    slices, in byte-wise name order, stacked along z into a uint8 Volume
+    [z, y, x].  The slices are decoded by libfasttau's TIFF reader
+    (fast_tiff_folder_info / fast_tiff_folder_read).  ``binarize=True``
+    applies Volume::binarize(threshold) on the GPU afterwards, which is what
+    `fast tau` does with a folder input (VolumeIOModule.h:57-63)."""
+    import ctypes as C
+
+    from . import _native
+    from .tau import Status
+
+    L = _native.lib()
+    path = os.fsencode(folder)
+    nx, ny, nz = C.c_int64(), C.c_int64(), C.c_int64()
+    st = L.fast_tiff_folder_info(path, C.byref(nx), C.byref(ny), C.byref(nz))
+    if st != Status.OK:
+        raise OSError(f"Failed to load {folder} ({Status(st).name}): {_native.last_error()}")
+    arr = np.empty((nz.value, ny.value, nx.value), np.uint8)
+    st = L.fast_tiff_folder_read(path, arr.ctypes.data_as(C.c_void_p), arr.nbytes)
+    if st != Status.OK:
+        raise OSError(f"Failed to load {folder} ({Status(st).name}): {_native.last_error()}")
+    vol = Volume(arr)
+    if binarize:
+        vol.binarize(threshold)
+    return vol
+
+
+__all__ = ["load_volume_binary", "save_volume_binary", "load_tiff_folder", "PRIMITIVE_TYPES"]

@@ -43,7 +43,8 @@ typedef enum fast_status {
     FAST_DIVERGED = 5,      /* |r|^2 > 1e11 in reference units (CG.cu:152, BICGSTAB.cu:207) */
     FAST_CUDA_ERROR = 6,    /* a CUDA call failed; the context stays usable */
     FAST_TIMEOUT = 7,       /* a bounded device-side wait ran out */
-    FAST_BAD_ARG = 8        /* invalid dimension / direction / solver / precision */
+    FAST_BAD_ARG = 8,       /* invalid dimension / direction / solver / precision */
+    FAST_IO_ERROR = 9       /* a volume file or folder cannot be read (VolumeIO.cpp:197-254) */
 } fast_status;
 
 /* enum Dir (fastlib/include/fastlib/utility/PrimitiveTypes.h:142-150). */
@@ -273,6 +274,36 @@ FAST_API int fast_ccl_label_device(const uint8_t *d_mask, int64_t nx, int64_t ny
  * bytes) as fast_ccl_label fills it. */
 FAST_API int fast_ccl_boundary_device(const uint32_t *d_labels, int64_t nx, int64_t ny, int64_t nz,
                                       uint32_t num_labels, uint8_t *boundary, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Volume input: TIFF folders and binarize                                   */
+/* ------------------------------------------------------------------------ */
+
+/* The scan of loadTiffFolder (fastlib/src/volume/VolumeIO.cpp:197-235): the
+ * dimensions of the volume a folder of 2D slices makes.  nx, ny = the first
+ * slice's width and height in byte-wise name order, nz = the number of files
+ * named *.tif or *.tiff (case-sensitive, as checkExtension).  Slices are
+ * baseline TIFF: uncompressed strips, 8-bit unsigned samples, either byte
+ * order; sample 0 of multi-sample pixels is read.  Other forms give
+ * FAST_BAD_TYPE (not 8-bit unsigned) or FAST_IO_ERROR.  Host-only work. */
+FAST_API int fast_tiff_folder_info(const char *folder, int64_t *nx, int64_t *ny, int64_t *nz);
+
+/* loadTiffFolder's reads (VolumeIO.cpp:237-248): slice z of the folder (name
+ * order) into out + z*nx*ny, rows y-major, x fastest; capacity = bytes of
+ * out.  Slices whose size differs from the first give FAST_IO_ERROR.  The
+ * voxels are the slices' raw values: the reference's TIFF input binarizes
+ * them next (fast_binarize). */
+FAST_API int fast_tiff_folder_read(const char *folder, uint8_t *out, uint64_t capacity);
+
+/* Volume::binarize(threshold) on a uint8 volume (fastlib/src/volume/
+ * Volume.cpp:478-486, kernelBinarizeUnsigned in fastlib/src/cuda/Volume.cu:
+ * 157-183): v = v < t ? 0 : 255 with t = uchar(threshold * 255) (threshold
+ * clamped to [0, 1] first; the reference's `fast tau` passes 1.0, so only 255
+ * stays 255).  Runs on the GPU.  fast_binarize takes a HOST volume of n bytes
+ * (copied in and back); fast_binarize_device a DEVICE one on `stream` (a
+ * cudaStream_t as void*, NULL = legacy default stream; not synchronised). */
+FAST_API int fast_binarize(uint8_t *volume, uint64_t n, float threshold);
+FAST_API int fast_binarize_device(uint8_t *d_volume, uint64_t n, float threshold, void *stream);
 
 /* Message of the calling thread's last failure ("" if none). */
 FAST_API const char *fast_last_error(void);

@@ -170,3 +170,16 @@ def ccl_boundary(labels, num_labels):
     out = np.empty((7, num_labels), dtype=np.uint8)
     lib().oracle_ccl_boundary(_ptr(labels), nx, ny, nz, num_labels, _ptr(out))
     return out
+
+
+def binarize(vol, threshold=1.0):
+    """Volume::binarize on uint8 (fastlib/src/volume/Volume.cpp:478-486,
+    kernelBinarizeUnsigned and launchBinarizeKernel in fastlib/src/cuda/
+    Volume.cu:157-183): t = uchar(threshold*255); v < t -> 0, else 255
+    (T(-1) for uchar).  The threshold is clamped to [0, 1] before the
+    conversion."""
+    t = float(np.float32(min(max(float(threshold), 0.0), 1.0)) * np.float32(255.0))
+    t = int(t)
+    v = np.asarray(vol, dtype=np.uint8)
+    return np.where(v < t, 0, 255).astype(np.uint8)
+
