@@ -680,6 +680,83 @@ def run_c5(args):
     print(json.dumps(line), flush=True)
 
 
+def run_alpha(args):
+    """Reactive area (`fast alpha`) on the large volume: 1024^3 spheres (seed
+    7, r = 10, solid 0.65), device-resident.  Timed (CUDA events, after
+    warm-up): the labelling of the pore phase alone, the full tensor call
+    (labelling + one seven-field marching-cubes pass), and the one-field
+    area pass.  The one-field pass reads 1 B per voxel (the mask); the
+    seven-field pass reads 5 B per voxel (mask + 32-bit label; the per-label
+    face bits stay in L2).  CPU baseline: the oracle's area of the same field
+    on a bounded 256^3 corner of the volume, all host threads."""
+    import ctypes as C
+    import torch
+    from fast_gb300 import _native, alpha, ccl, volumes
+    from oracle import oracle as O
+    n = args.c5_edge
+    m = volumes.spheres((n, n, n), seed=7, r_min=10.0, solid_fraction=0.65)
+    sample = np.ascontiguousarray(m[:256, :256, :256]) if not args.no_cpu_baseline else None
+    d_mask = torch.from_numpy(m).cuda()
+    del m
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    N = n ** 3
+    d_labels = torch.empty((n, n, n), dtype=torch.int32, device="cuda")
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        e0, e1 = _events(stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    ms_ccl = timed(lambda: ccl.get_volume_ccl_device(d_mask.data_ptr(), (n, n, n), d_labels.data_ptr(),
+                                                     background=255))
+    del d_labels
+    torch.cuda.empty_cache()
+    out = {}
+
+    def tensor():
+        out["t"] = alpha.get_reactive_area_density_tensor_device(d_mask.data_ptr(), (n, n, n), 0.5, sp)
+
+    ms_tensor = timed(tensor)
+    one = C.c_double()
+    L = _native.lib()
+
+    def area1():
+        L.fast_reactive_area_device(C.c_void_p(d_mask.data_ptr()), n, n, n, 0.5, C.byref(one), C.c_void_p(sp))
+
+    ms_area1 = timed(area1)
+    t, solid = out["t"]
+    peak, kind = load_peaks()
+    ms_area7 = max(ms_tensor - ms_ccl, 1e-9)
+    cpu = None
+    if sample is not None:
+        import multiprocessing
+        t0 = time.perf_counter()
+        a_cpu = O.reactive_area(sample)
+        dt = time.perf_counter() - t0
+        cpu = {"value": sample.size / dt, "unit": "voxels/s", "cores": multiprocessing.cpu_count(), "kind": "port",
+               "sample": "oracle area of the solid field on the 256^3 corner of the volume", "area": a_cpu}
+    line = _line("reactive area voxels/s", N / (ms_tensor / 1e3), "voxels/s", args, ms_tensor, "u8+u32->f32/f64",
+                 {"workload": f"alpha_spheres{n}_tensor", "volume": f"{n}^3 spheres seed 7 r=10 solid 0.65",
+                  "isovalue": 0.5, "inputs": "device-resident, larger than L2"},
+                 tensor=t, area_solid=solid, area_one_field=one.value,
+                 ms={"labelling": ms_ccl, "tensor_total": ms_tensor, "area_pass_7_fields": ms_area7,
+                     "area_pass_1_field": ms_area1},
+                 roofline={"bound": "hbm", "kernel": "alpha_kernel<false>", "achieved": N / (ms_area1 / 1e3) / 1e9,
+                           "peak": peak, "unit": "GB/s", "frac": N / (ms_area1 / 1e3) / 1e9 / peak,
+                           "peak_kind": kind, "bytes_per_voxel": 1,
+                           "seven_field_gbs_at_5B": 5 * N / (ms_area7 / 1e3) / 1e9},
+                 cpu_baseline=cpu)
+    print(json.dumps(line), flush=True)
+
+
 def run_ncu_case(args):
     """A short, fixed run of the workload's kernels for profiler captures:
     the bench volume, one direction (x), MIXED BiCGSTAB (or CG with
@@ -709,7 +786,7 @@ def main():
                     help="run a short fixed slice of the workload for profiler captures and exit")
     ap.add_argument("--ncu-iters", type=int, default=12)
     ap.add_argument("--ncu-solver", default="bicgstab", choices=["bicgstab", "cg"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "alpha"],
                     help="c2 (default) is the headline; the others print their own line")
     ap.add_argument("--requests", type=int, default=64, help="c4: requests in the stream")
     ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 2000.0], help="c4: arrival rates (1/s)")
@@ -727,7 +804,7 @@ def main():
         build.build()
         import torch
         torch.cuda.set_device(0)
-        {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
+        {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5, "alpha": run_alpha}[args.workload](args)
         return
     ws, rank, local = dist_init()
     if args.impl == "reference":

@@ -21,7 +21,7 @@ LIB = os.path.join(OUT, "libfasttau.so")
 CLI = os.path.join(OUT, "fast")  # the `fast tau` command-line drop-in
 
 CUDA_SOURCES = ["kern_f64.cu", "kern_f32.cu", "kern_misc.cu", "tau_host.cu", "noalloc.cu", "ccl.cu", "serve.cu",
-                "volume_ops.cu"]
+                "volume_ops.cu", "alpha.cu"]
 CXX_SOURCES = ["gen.cpp", "tiff_folder.cpp"]
 CLI_SOURCE = "fast_cli.cpp"
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,6 +1,17 @@
-// `fast tau`: the command-line drop-in for the reference's tortuosity action
-// (fast/src/main.cpp, fast/src/TauModule.h:14-153, VolumeIOModule.h:139-253,
+// `fast tau` and `fast alpha`: the command-line drop-in for the reference's
+// tortuosity and reactive-area actions (fast/src/main.cpp,
+// fast/src/TauModule.h:14-153, AlphaModule.h:8-233, VolumeIOModule.h:139-253,
 // CSVOutputModule.h:35-112), over libfasttau.so's C ABI.
+//
+//   fast alpha <input.bin|tiff folder> [-d ...] [--basic] [crops] [-o out.csv]
+//
+// alpha rows (AlphaModule::getAlpha, AlphaModule.h:28-179): without --basic,
+// one row per direction with the area of the pore space connected to that
+// face (rad; radTime = the labelling + tensor time / 6) and a DIR_NONE row
+// with the whole solid/pore area; with --basic, one row per direction
+// carrying the whole area (radBasic, radBasicTime) and no dir column.
+// Columns are sorted by name as the reference's row map sorts them.  --mesh
+// (OBJ export) and --segmentinfo are not provided.
 //
 //   fast tau <input.bin|tiff folder> [-d x|y|z|xy..|all|pos|neg|xneg|yneg|zneg]
 //            [--solver CG|BICGSTAB] [--tol N] [--iter N] [-p d|f|mixed]
@@ -54,7 +65,9 @@ int usage(const char *why)
     if (why) std::cerr << "error: " << why << "\n";
     std::cerr << "usage: fast tau <input.bin|tiff folder> [-d x|y|z|all|pos|neg] [--solver CG|BICGSTAB] [--tol N]\n"
                  "                [--iter N] [-p d|f|mixed] [--sub x,y,z] [--origin x,y,z] [--randsub x,y,z]\n"
-                 "                [--aspect x,y,z] [-o out.csv] [-v] [--cpu] [-j N]\n";
+                 "                [--aspect x,y,z] [-o out.csv] [-v] [--cpu] [-j N]\n"
+                 "       fast alpha <input.bin|tiff folder> [-d x|y|z|all|pos|neg] [--basic] [--sub x,y,z]\n"
+                 "                [--origin x,y,z] [--randsub x,y,z] [--aspect x,y,z] [-o out.csv]\n";
     return why ? 1 : 0;
 }
 
@@ -220,6 +233,106 @@ void write_row(const std::string &out_path, bool &first_stdout, const Row &r)
     f << line.str();
 }
 
+// CSVOutputModule::addRunRow for a row map: columns sorted by name, header
+// when the output is new.
+void write_map_row(const std::string &out_path, bool &first_stdout,
+                   std::vector<std::pair<std::string, std::string>> row)
+{
+    std::sort(row.begin(), row.end());
+    std::ostringstream header, line;
+    for (size_t k = 0; k < row.size(); k++) {
+        header << (k ? "," : "") << row[k].first;
+        line << (k ? "," : "") << row[k].second;
+    }
+    header << "\n";
+    line << "\n";
+    if (out_path.empty()) {
+        if (first_stdout) std::cout << header.str();
+        first_stdout = false;
+        std::cout << line.str();
+        std::cout.flush();
+        return;
+    }
+    bool is_new;
+    {
+        std::ifstream f(out_path);
+        is_new = !f.is_open();
+    }
+    std::ofstream f(out_path, std::ios::app);
+    if (is_new) f << header.str();
+    f << line.str();
+}
+
+template <typename T>
+std::string fmt(T v)
+{
+    std::ostringstream o;
+    o << v;
+    return o.str();
+}
+
+// AlphaModule::getAlpha (AlphaModule.h:28-179) without the mesh and
+// segment-info exports.
+int run_alpha(const std::string &name, const Vol &vol, const std::vector<int32_t> &dirs, bool basic,
+              const std::string &out_path)
+{
+    double phi = 0.0;
+    if (fast_porosity(vol.data.data(), vol.nx, vol.ny, vol.nz, &phi, nullptr) != FAST_OK) {
+        std::cerr << "error: " << fast_last_error() << "\n";
+        return 1;
+    }
+    const std::vector<std::pair<std::string, std::string>> common = {
+        {"ID", name}, {"dimx", fmt(vol.nx)}, {"dimy", fmt(vol.ny)}, {"dimz", fmt(vol.nz)},
+        {"porosity", fmt((float)phi)}};
+    bool first_stdout = true;
+    auto timed_area = [&](double *area, double *secs) {
+        const auto t0 = std::chrono::system_clock::now();
+        const int st = fast_reactive_area(vol.data.data(), vol.nx, vol.ny, vol.nz, 0.5f, area);
+        *secs = std::chrono::duration<double>(std::chrono::system_clock::now() - t0).count();
+        return st;
+    };
+    if (!basic) {
+        double tensor[6], solid = 0.0;
+        const auto t0 = std::chrono::system_clock::now();
+        int st = fast_reactive_area_tensor(vol.data.data(), vol.nx, vol.ny, vol.nz, 0.5f, tensor, &solid);
+        const double rad_time = std::chrono::duration<double>(std::chrono::system_clock::now() - t0).count();
+        if (st != FAST_OK) {
+            std::cerr << "error: " << fast_last_error() << "\n";
+            return 1;
+        }
+        for (int32_t d : dirs) {
+            auto row = common;
+            row.push_back({"rad", fmt(tensor[d])});
+            row.push_back({"radTime", fmt(rad_time / 6.0f)});
+            row.push_back({"dir", dir_string(d)});
+            write_map_row(out_path, first_stdout, row);
+        }
+        double area = 0.0, secs = 0.0;
+        if ((st = timed_area(&area, &secs)) != FAST_OK) {
+            std::cerr << "error: " << fast_last_error() << "\n";
+            return 1;
+        }
+        auto row = common;
+        row.push_back({"rad", fmt((float)area)});
+        row.push_back({"radTime", fmt(secs)});
+        row.push_back({"dir", "DIR_NONE"});
+        write_map_row(out_path, first_stdout, row);
+    } else {
+        double area = 0.0, secs = 0.0;
+        if (timed_area(&area, &secs) != FAST_OK) {
+            std::cerr << "error: " << fast_last_error() << "\n";
+            return 1;
+        }
+        for (size_t k = 0; k < dirs.size(); k++) {
+            auto row = common;
+            row.push_back({"radBasic", fmt((float)area)});
+            row.push_back({"radBasicTime", fmt(secs)});
+            write_map_row(out_path, first_stdout, row);
+        }
+    }
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -227,7 +340,8 @@ int main(int argc, char **argv)
     if (argc < 2) return usage("missing action");
     const std::string action = argv[1];
     if (action == "-h" || action == "--help") return usage(nullptr);
-    if (action != "tau") return usage("only the `tau` action is built");
+    if (action != "tau" && action != "alpha") return usage("only the `tau` and `alpha` actions are built");
+    bool basic = false;
 
     std::string input, dir = "x-", solver = "CG", precision = "double", out_path;
     int tol_exp = 6;
@@ -253,6 +367,11 @@ int main(int argc, char **argv)
         else if (a == "-o" || a == "--output") out_path = next("-o");
         else if (a == "-v" || a == "--verbose") verbose = true;
         else if (a == "--cpu" || a == "--over" || a == "--oversubscribe") { /* accepted, no effect */ }
+        else if (a == "--basic" && action == "alpha") basic = true;
+        else if ((a == "--mesh" || a == "--segmentinfo") && action == "alpha") {
+            std::cerr << "error: " << a << " is not provided\n";
+            return 1;
+        }
         else if (a == "-j" || a == "--cputhreads") next("-j");
         else if (a == "--sub") has_sub = parse3(next("--sub"), sub);
         else if (a == "--origin") has_origin = parse3(next("--origin"), origin);
@@ -319,6 +438,8 @@ int main(int argc, char **argv)
         const int64_t lo[3] = {0, 0, 0};
         vol = crop(vol, lo, size);
     }
+
+    if (action == "alpha") return run_alpha(input, vol, get_dirs(dir), basic, out_path);
 
     fast_tau_params p;
     fast_tau_params_init(&p);

@@ -305,6 +305,42 @@ FAST_API int fast_tiff_folder_read(const char *folder, uint8_t *out, uint64_t ca
 FAST_API int fast_binarize(uint8_t *volume, uint64_t n, float threshold);
 FAST_API int fast_binarize_device(uint8_t *d_volume, uint64_t n, float threshold, void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* Reactive area density (`fast alpha`)                                       */
+/* ------------------------------------------------------------------------ */
+
+/* getReactiveAreaDensity<T>(mask, mask.dim(), isovalue) (fastlib/src/volume/
+ * VolumeMeasures.cpp:294-301 over getVolumeArea, VolumeSurface.cpp:10-36, and
+ * the marching-cubes cell kernel, fastlib/src/cuda/VolumeSurface.cu:198-262):
+ * the area of the isovalue surface of the volume read as v/255 at the cell
+ * corners (each corner = mean of the 2x2x2 voxels around it, clamped at the
+ * faces), in normalized units (axis a scaled by 1/n_a), summed in double.
+ * The mask must hold 0 and 255 only (FAST_BAD_TYPE otherwise); `fast alpha`
+ * uses isovalue 0.5.  The triangulation table is the engine's own (see
+ * alpha.cu): areas of cells whose loop is not planar differ slightly from the
+ * reference's table.  Host mask; synchronous. */
+FAST_API int fast_reactive_area(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, float isovalue,
+                                double *area);
+
+/* The same on a DEVICE mask; stream: a cudaStream_t as void*, NULL = the
+ * legacy default stream; the call synchronises it. */
+FAST_API int fast_reactive_area_device(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, float isovalue,
+                                       double *area, void *stream);
+
+/* getVolumeCCL(mask, 255) + getReactiveAreaDensityTensor<T>(ccl, dims,
+ * isovalue) (VolumeMeasures.cpp:303-335, generateBoundaryConnectedVolume in
+ * VolumeSegmentation.cpp:66-90): tensor[d] (6 doubles, Dir order) = the area
+ * of the pore space (voxels != 255) whose component touches face d.  The
+ * solid/pore area of fast_reactive_area comes from the same pass into
+ * *area_solid (nullable).  One labelling and one area pass for all seven.
+ * Volumes of 4294967295 voxels or more are rejected (labels are 32-bit). */
+FAST_API int fast_reactive_area_tensor(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, float isovalue,
+                                       double *tensor, double *area_solid);
+
+/* The same on a DEVICE mask (stream as above; synchronised). */
+FAST_API int fast_reactive_area_tensor_device(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz,
+                                              float isovalue, double *tensor, double *area_solid, void *stream);
+
 /* Message of the calling thread's last failure ("" if none). */
 FAST_API const char *fast_last_error(void);
 

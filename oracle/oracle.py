@@ -1,4 +1,4 @@
-"""ctypes front end of the CPU oracle (tau_oracle.c, ccl_oracle.c).
+"""ctypes front end of the CPU oracle (tau_oracle.c, ccl_oracle.c, alpha_oracle.c).
 
 TEST INFRASTRUCTURE ONLY.  tests/, the smoke check and bench.py's CPU
 baseline leg use this module as the checker for the CUDA path; the product
@@ -34,7 +34,8 @@ D1_F32 = float(np.float32(0.001))
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, OpenMP)."""
-    srcs = [os.path.join(_HERE, f) for f in ("tau_oracle.c", "tau_oracle_impl.h", "ccl_oracle.c")]
+    srcs = [os.path.join(_HERE, f) for f in ("tau_oracle.c", "tau_oracle_impl.h", "ccl_oracle.c", "alpha_oracle.c",
+                                             "Makefile")]
     if not force and os.path.exists(_SO):
         so_m = os.path.getmtime(_SO)
         if all(os.path.getmtime(s) <= so_m for s in srcs):
@@ -70,6 +71,10 @@ def lib():
             L.oracle_ccl_label.argtypes = [P, i64, i64, i64, C.c_uint8, P]
             L.oracle_ccl_label.restype = C.c_uint32
             L.oracle_ccl_boundary.argtypes = [P, i64, i64, i64, C.c_uint32, P]
+            L.oracle_area_field.argtypes = [P, i64, i64, i64, f32]
+            L.oracle_area_field.restype = f64
+            L.oracle_mc_ntri.argtypes = [i32]
+            L.oracle_mc_ntri.restype = i32
             _lib = L
     return _lib
 
@@ -182,4 +187,27 @@ def binarize(vol, threshold=1.0):
     t = int(t)
     v = np.asarray(vol, dtype=np.uint8)
     return np.where(v < t, 0, 255).astype(np.uint8)
+
+
+def area_field(field, iso=0.5) -> float:
+    """Marching-cubes area of the isovalue surface of a 0/1 field [z, y, x]
+    (getVolumeArea + sum, VolumeSurface.cpp:10-36, VolumeMeasures.cpp:294-301)."""
+    f = np.ascontiguousarray(field, dtype=np.uint8)
+    nx, ny, nz = _dims(f)
+    return float(lib().oracle_area_field(_ptr(f), nx, ny, nz, float(iso)))
+
+
+def reactive_area(mask, iso=0.5) -> float:
+    """getReactiveAreaDensity(mask, mask.dim(), iso) on a 0/255 mask."""
+    return area_field(np.asarray(mask) != 0, iso)
+
+
+def reactive_area_tensor(mask, iso=0.5):
+    """getVolumeCCL(mask, 255) + getReactiveAreaDensityTensor: for each Dir d
+    the area of the pore components (voxels != 255) touching face d
+    (generateBoundaryConnectedVolume, VolumeSegmentation.cpp:66-90)."""
+    mask = np.ascontiguousarray(mask, dtype=np.uint8)
+    labels, n = ccl_label(mask, 255)
+    table = ccl_boundary(labels, n)
+    return [area_field(table[d][labels], iso) for d in range(6)]
 
