@@ -34,7 +34,16 @@ void launch_code(const Launch &L, cudaStream_t st) { code_kernel<<<(unsigned)L.n
 void launch_tau(int src, const Launch &L, cudaStream_t st)
 {
     if (src == 1) tau_kernel<float><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, 0);
-    else tau_kernel<double><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, src == 2 ? 1 : 0);
+    else if (src == 2) tau_kernel<FF><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, 1);
+    else tau_kernel<double><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, 0);
+}
+
+void launch_ff_to_double(const void *src, double *dst, int64_t n, cudaStream_t st)
+{
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    if (blocks < 1) blocks = 1;
+    ff_to_double_kernel<<<(unsigned)blocks, 256, 0, st>>>((const float2 *)src, dst, n);
 }
 
 }  // namespace ft

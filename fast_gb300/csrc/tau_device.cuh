@@ -10,6 +10,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <type_traits>
 #include "tau_types.h"
 
 namespace ft {
@@ -31,6 +32,19 @@ namespace ft {
 // table is the interior diagonal they use).
 // ---------------------------------------------------------------------------
 constexpr int NBC = 7;  // boundary counts -2..4
+
+// Float-float number: value = hi + lo, |lo| <= ulp(hi) / 2, about 48
+// significant bits.  The MIXED residual replacement keeps its iterate and
+// evaluates b - A x in this form with FP32 instructions (error-free
+// transformations: Knuth's two-sum, Dekker's product through a fused
+// multiply-add), because FP64 throughput on this GPU is a small fraction of
+// FP32's.
+struct FF {
+    float hi, lo;
+    FF() = default;
+    __host__ __device__ constexpr FF(int v) : hi((float)v), lo(0.f) {}
+    __host__ __device__ constexpr FF(float h, float l) : hi(h), lo(l) {}
+};
 
 template <typename T>
 struct Coef {
@@ -61,6 +75,26 @@ __device__ __forceinline__ void load_coef(Coef<T> &C, const Job &J, int tid)
     }
 }
 
+// The replacement's tables: the FP64 coefficients as float-float pairs.
+template <>
+struct Coef<FF> {
+    static constexpr int NB = NBC;
+    FF face[2][2];
+    FF cell2[2];
+    float dhi[NBC][128], dlo[NBC][128];  // diagonal by (boundary count + 2, code)
+};
+
+template <>
+__device__ __forceinline__ void load_coef<FF>(Coef<FF> &C, const Job &J, int tid)
+{
+    for (int k = tid; k < NBC * 128; k += NTHREADS) {
+        C.dhi[k >> 7][k & 127] = J.xdiag_hi[k >> 7][k & 127];
+        C.dlo[k >> 7][k & 127] = J.xdiag_lo[k >> 7][k & 127];
+    }
+    if (tid < 4) C.face[tid >> 1][tid & 1] = FF(J.xface[tid >> 1][tid & 1][0], J.xface[tid >> 1][tid & 1][1]);
+    if (tid < 2) C.cell2[tid] = FF(J.xcell2[tid][0], J.xcell2[tid][1]);
+}
+
 // Face coefficients of a solve, held in registers by every thread.
 template <typename T>
 struct Faces {
@@ -70,8 +104,14 @@ struct Faces {
 template <typename T>
 __device__ __forceinline__ Faces<T> faces_of(const Job &J)
 {
-    if constexpr (sizeof(T) == 8) return Faces<T>{J.dface[0][0], J.dface[0][1], J.dface[1][0], J.dface[1][1]};
-    else return Faces<T>{J.fface[0][0], J.fface[0][1], J.fface[1][0], J.fface[1][1]};
+    if constexpr (std::is_same<T, FF>::value) {
+        auto f = [&](int s, int n) { return FF(J.xface[s][n][0], J.xface[s][n][1]); };
+        return Faces<T>{f(0, 0), f(0, 1), f(1, 0), f(1, 1)};
+    } else if constexpr (sizeof(T) == 8) {
+        return Faces<T>{J.dface[0][0], J.dface[0][1], J.dface[1][0], J.dface[1][1]};
+    } else {
+        return Faces<T>{J.fface[0][0], J.fface[0][1], J.fface[1][0], J.fface[1][1]};
+    }
 }
 
 // A voxel of a sweep: coordinates and its boundary count (see above).
@@ -219,6 +259,11 @@ __device__ __forceinline__ T stencil7(const Faces<T> &F, uint32_t code, T fc, T 
     return s;
 }
 
+// The same stencil in float-float arithmetic (the MIXED residual
+// replacement), same summation order; `diag` from the float-float table.
+__device__ __forceinline__ FF stencil7_ff(const Faces<FF> &F, uint32_t code, FF fc, FF fxp, FF fxm, FF fyp, FF fym,
+                                          FF fzp, FF fzm, FF diag);
+
 // ---------------------------------------------------------------------------
 // Dot-product accumulation.  FP64 solves accumulate in double.  FP32 solves
 // accumulate each thread's products in FP32 (at most one slab column, a few
@@ -263,6 +308,74 @@ __device__ __forceinline__ void pair_add(float &s, float &c, float s2, float c2)
     two_sum(s, s2, t, e);
     s = t;
     c = __fadd_rn(__fadd_rn(c, c2), e);
+}
+
+// Float-float arithmetic (value = hi + lo).
+// (s, e) -> (hi, lo) with hi = fl(s + e); a full two-sum, since near a
+// converged residual e need not be smaller than s.
+__device__ __forceinline__ FF ff_renorm(float s, float e)
+{
+    float h, l;
+    two_sum(s, e, h, l);
+    return FF(h, l);
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    return ff_renorm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ FF ff_add_f(FF a, float b)
+{
+    float s, e;
+    two_sum(a.hi, b, s, e);
+    return ff_renorm(s, __fadd_rn(e, a.lo));
+}
+
+__device__ __forceinline__ FF ff_neg(FF a) { return FF(-a.hi, -a.lo); }
+__device__ __forceinline__ FF operator-(FF a) { return ff_neg(a); }
+
+__device__ __forceinline__ float ff_to_float(FF a) { return __fadd_rn(a.hi, a.lo); }
+
+// Accumulator of a sum of float-float products: hi parts in an error-free
+// two-sum chain, every error and low-order term in one float, normalised once.
+struct FFSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add_prod(FF a, FF b)
+    {
+        const float p = __fmul_rn(a.hi, b.hi);
+        float pl = __fmaf_rn(a.hi, b.hi, -p);  // exact error of the product
+        pl = __fmaf_rn(a.hi, b.lo, pl);
+        pl = __fmaf_rn(a.lo, b.hi, pl);
+        float t, e;
+        two_sum(s, p, t, e);
+        s = t;
+        c = __fadd_rn(c, __fadd_rn(e, pl));
+    }
+    __device__ __forceinline__ FF value() const { return ff_renorm(s, c); }
+};
+
+__device__ __forceinline__ FF stencil7_ff(const Faces<FF> &F, uint32_t code, FF fc, FF fxp, FF fxm, FF fyp, FF fym,
+                                          FF fzp, FF fzm, FF diag)
+{
+    const bool solid = (code >> SELF_BIT) & 1;
+    const FF a = solid ? F.a1 : F.a0, b = solid ? F.b1 : F.b0;
+    FFSum s;
+    s.add_prod(fxp, (code & 1) ? b : a);
+    s.add_prod(fxm, (code & 2) ? b : a);
+    s.add_prod(fyp, (code & 4) ? b : a);
+    s.add_prod(fym, (code & 8) ? b : a);
+    s.add_prod(fzp, (code & 16) ? b : a);
+    s.add_prod(fzm, (code & 32) ? b : a);
+    s.add_prod(fc, diag);
+    return s.value();
+}
+
+__device__ __forceinline__ FF diag_ff(const Coef<FF> &C, uint32_t code, const Pos &p)
+{
+    return FF(C.dhi[p.bc + 2][code & 127], C.dlo[p.bc + 2][code & 127]);
 }
 
 // Sum NV per-thread values over the block (fixed tree) and store the block

@@ -221,6 +221,20 @@ void fill_tables(Job &J, double d0, double d1, int face_mean)
             J.finv_b[bc + 2][code] = 1.0f / d;
         }
     }
+    // Float-float splits (hi = nearest float, lo = nearest float of the rest).
+    auto split = [](double v, float &hi, float &lo) {
+        hi = (float)v;
+        lo = (float)(v - (double)hi);
+    };
+    for (int s = 0; s < 2; s++) {
+        split(2.0 * Dd[s], J.xcell2[s][0], J.xcell2[s][1]);
+        for (int n = 0; n < 2; n++) split(J.dface[s][n], J.xface[s][n][0], J.xface[s][n][1]);
+    }
+    for (int code = 0; code < 128; code++) {
+        const int self = (code >> SELF_BIT) & 1;
+        for (int bc = -2; bc <= 4; bc++)
+            split(J.ddiag_int[code] + Dd[self] * (double)bc, J.xdiag_hi[bc + 2][code], J.xdiag_lo[bc + 2][code]);
+    }
     J.c_tau[0] = (float)d0;
     J.c_tau[1] = (float)d1;
 }
@@ -484,8 +498,8 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
         J.v[1] = A.take(vbytes);
     }
     if (mixed) {
-        J.x64[0] = (double *)A.take(v64);
-        J.x64[1] = (double *)A.take(v64);
+        J.x64[0] = A.take(v64);
+        J.x64[1] = A.take(v64);
         if (solver == FAST_SOLVER_BICGSTAB) J.t = A.take(vbytes);
     }
     J.part = (double *)A.take((size_t)G.ntiles * NPART * sizeof(double));
@@ -653,7 +667,13 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
         size_t es = vec_t;
         CU(cudaStreamSynchronize(st));
         if (mixed) {
-            src = hj[0].x64[hs[0].x64_cur];
+            // The iterate is float-float: widen it to FP64 in the other
+            // ping-pong buffer (free now), then copy that.
+            const int cur = hs[0].x64_cur;
+            const int64_t n = (int64_t)hj[0].pitch * vols[0].ny * vols[0].nz;
+            launch_ff_to_double(hj[0].x64[cur], (double *)hj[0].x64[cur ^ 1], n, st);
+            CU(cudaGetLastError());
+            src = hj[0].x64[cur ^ 1];
             es = 8;
         }
         // de-pad the rows: host layout is x-fastest with pitch nx
@@ -939,7 +959,8 @@ FAST_API int fast_porosity(const uint8_t *mask, int64_t nx, int64_t ny, int64_t 
     const size_t NP = (size_t)(P * ny * nz);
     cudaStream_t s = E->stream;
     Arena A;
-    const size_t need = align_up(N, 256) + align_up(NP, 256) + align_up((size_t)G.ntiles * NPART * 8, 256) + 4 * 4096;
+    const size_t need = align_up(N, 256) + align_up(NP, 256) + align_up((size_t)G.ntiles * NPART * 8, 256) +
+                        align_up(sizeof(Scalars), 256) + align_up(sizeof(uint32_t), 256) + align_up(sizeof(Job), 256);
     CU(cudaMallocAsync((void **)&A.base, need, s));
     uint8_t *d_mask = (uint8_t *)A.take(N);
     uint8_t *d_code = (uint8_t *)A.take(NP);

@@ -22,6 +22,8 @@ void launch_init64(const Launch &L, cudaStream_t st);
 void launch_code(const Launch &L, cudaStream_t st);
 // tau flux sum: src 0 = double x, 1 = float x, 2 = the current FP64 iterate.
 void launch_tau(int src, const Launch &L, cudaStream_t st);
+// n float-float pairs at src -> n doubles at dst (device).
+void launch_ff_to_double(const void *src, double *dst, int64_t n, cudaStream_t st);
 // Raise the dynamic shared-memory limit of every sweep kernel (once per device).
 cudaError_t configure_f64();
 cudaError_t configure_f32();

@@ -7,13 +7,16 @@
 namespace ft {
 
 // ===========================================================================
-// MIXED residual replacement (FP64).  The FP32 iterations work on a
-// correction e of the FP64 iterate x64; when one of them asks for it
-// (`replace`), this step folds e into x64 (x64' = x64 + e, e is zeroed by the
-// next step-1 kernel), recomputes the residual b - A x64' in FP64 and hands
+// MIXED residual replacement.  The FP32 iterations work on a correction e of
+// an extended-precision iterate x64 (a float-float pair per voxel, about 48
+// significant bits); when one of them asks for it (`replace`), this step
+// folds e into x64 (x64' = x64 + e, e is zeroed by the next step-1 kernel),
+// recomputes the residual b - A x64' in float-float arithmetic and hands
 // fp32 of it to the recursion in place of the recursive residual, keeping
 // the Krylov vectors (replace = 1) or restarting them from it (replace = 2,
 // also the first step of a solve).  The true residual decides convergence.
+// Float-float instead of FP64: the same role (a residual exact to far below
+// FP32 rounding, here about 1e-14 of |A||x|) with FP32 instructions only.
 // Dots, accumulated in FP32 per thread (they steer the iteration and test
 // convergence; they need no more than FP32 accuracy): |fp32(r64)|^2, |b|^2
 // and, for BiCGSTAB, r0.fp32(r64) (r0 = fp32(r64) itself on a restart), for
@@ -21,16 +24,17 @@ namespace ft {
 // ===========================================================================
 template <bool BICG>
 struct OpReplace {
-    using T = double;
+    using T = FF;
+    using R = double;
     using SL = typename std::conditional<BICG, Streams<8, 4, 1, 4>, Streams<8, 4, 1>>::type;
     static constexpr int NV = 3;
     using Shared = Coef<float>;
-    struct Vals { double x; float e; uint32_t code; float r0; };
+    struct Vals { FF x; float e; uint32_t code; float r0; };
     struct Own { uint32_t code; float r0; };
-    struct Out { double x; float r; };
+    struct Out { FF x; float r; };
     const CUtensorMap *tmap[SL::N];
     Faces<T> F;
-    double *x64n;
+    FF *x64n;
     float *r, *r0, *p, *v;
     bool restart;
     Acc<float> a_rr, a_bb, a_d;
@@ -39,14 +43,14 @@ struct OpReplace {
     __device__ static void load_shared(Shared &S, const Job &J, int tid) { load_coef<float>(S, J, tid); }
     __device__ static void load2(const unsigned char *st, const Pt &p_, Vals &a, Vals &b)
     {
-        sv2<double, SL, 0>(st, p_, a.x, b.x);
+        sv2<FF, SL, 0>(st, p_, a.x, b.x);
         sv2<float, SL, 1>(st, p_, a.e, b.e);
         load_code2<SL, 2>(st, p_, a.code, b.code);
         if constexpr (BICG) sv2<float, SL, 3>(st, p_, a.r0, b.r0);
     }
     __device__ static void load1(const unsigned char *st, const Pt &p_, Vals &a)
     {
-        a.x = sv<double, SL, 0>(st, p_);
+        a.x = sv<FF, SL, 0>(st, p_);
         a.e = sv<float, SL, 1>(st, p_);
     }
     __device__ void init(const Job &J, Shared &)
@@ -59,31 +63,29 @@ struct OpReplace {
         tmap[1] = &J.tm[TM_X];
         tmap[2] = &J.tm[TM_CODE];
         if constexpr (BICG) tmap[3] = &J.tm[TM_R0];
-        x64n = J.x64[cur ^ 1];
+        x64n = (FF *)J.x64[cur ^ 1];
         r = (float *)J.r[par];
         r0 = (float *)J.r0;
         p = (float *)J.p[(int)(sc.iter & 1)];
         v = BICG ? (float *)J.v[par] : nullptr;
         restart = sc.replace == 2;
     }
-    __device__ double field(const Geo &, const Coef<double> &, Shared &, const Vals &a, const Pos &) const
+    __device__ FF field(const Geo &, const Coef<FF> &, Shared &, const Vals &a, const Pos &) const
     {
-        return a.x + (double)a.e;
+        return ff_add_f(a.x, a.e);
     }
-    __device__ Own own(const Geo &, const Coef<double> &, Shared &, const Vals &a, const Pos &, double &f) const
+    __device__ Own own(const Geo &, const Coef<FF> &, Shared &, const Vals &a, const Pos &, FF &f) const
     {
-        f = a.x + (double)a.e;
+        f = ff_add_f(a.x, a.e);
         return Own{a.code, a.r0};
     }
-    __device__ Out apply(const Geo &g, const Coef<double> &C, Shared &S, const Own &o, const Pos &ps,
-                         double fc, double fxp, double fxm, double fyp, double fym, double fzp, double fzm)
+    __device__ Out apply(const Geo &g, const Coef<FF> &C, Shared &S, const Own &o, const Pos &ps, FF fc, FF fxp,
+                         FF fxm, FF fyp, FF fym, FF fzp, FF fzm)
     {
-        const double d = diag_of<double, false>(C, g, o.code, ps);
-        const double ax = stencil7<double>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
-        const double b = rhs_at<double>(C, g, o.code, ps.x, ps.y, ps.z);
-        const double res = b - ax;
-        const float r32 = (float)res;
-        const float b32 = (float)b;
+        const FF ax = stencil7_ff(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag_ff(C, o.code, ps));
+        const FF b = rhs_at<FF>(C, g, o.code, ps.x, ps.y, ps.z);
+        const float r32 = ff_to_float(ff_add(b, ff_neg(ax)));
+        const float b32 = ff_to_float(b);
         a_rr.add_prod(r32, r32);
         a_bb.add_prod(b32, b32);
         if constexpr (BICG) {
@@ -96,7 +98,7 @@ struct OpReplace {
     }
     __device__ void store(int64_t i, const Out &a, const Out &b, bool v0_, bool v1_)
     {
-        store2<double>(x64n, i, a.x, b.x, v0_, v1_);
+        store2<FF>(x64n, i, a.x, b.x, v0_, v1_);
         store2<float>(r, i, a.r, b.r, v0_, v1_);
         if (restart) {
             store2<float>(p, i, 0.f, 0.f, v0_, v1_);
@@ -166,16 +168,17 @@ struct OpReplace {
 // Streams: x64, e, p, r, v, r0, code.
 // ===========================================================================
 struct OpReplaceBi2 {
-    using T = double;
+    using T = FF;
+    using R = double;
     using SL = Streams<8, 4, 4, 4, 4, 4, 1>;
     static constexpr int NV = 3;
     using Shared = Coef<float>;
-    struct Vals { double x; float e, p, r, v, r0; uint32_t code; };
+    struct Vals { FF x; float e, p, r, v, r0; uint32_t code; };
     struct Own { uint32_t code; float r0; };
-    struct Out { double x; float r; };
+    struct Out { FF x; float r; };
     const CUtensorMap *tmap[SL::N];
     Faces<T> F;
-    double *x64n;
+    FF *x64n;
     float *t, *r0;
     float alpha, omega;
     bool restart;
@@ -185,7 +188,7 @@ struct OpReplaceBi2 {
     __device__ static void load_shared(Shared &S, const Job &J, int tid) { load_coef<float>(S, J, tid); }
     __device__ static void load2(const unsigned char *st, const Pt &p_, Vals &a, Vals &b)
     {
-        sv2<double, SL, 0>(st, p_, a.x, b.x);
+        sv2<FF, SL, 0>(st, p_, a.x, b.x);
         sv2<float, SL, 1>(st, p_, a.e, b.e);
         sv2<float, SL, 2>(st, p_, a.p, b.p);
         sv2<float, SL, 3>(st, p_, a.r, b.r);
@@ -195,7 +198,7 @@ struct OpReplaceBi2 {
     }
     __device__ static void load1(const unsigned char *st, const Pt &p_, Vals &a)
     {
-        a.x = sv<double, SL, 0>(st, p_);
+        a.x = sv<FF, SL, 0>(st, p_);
         a.e = sv<float, SL, 1>(st, p_);
         a.p = sv<float, SL, 2>(st, p_);
         a.r = sv<float, SL, 3>(st, p_);
@@ -215,36 +218,35 @@ struct OpReplaceBi2 {
         tmap[4] = &J.tm[TM_V + par];
         tmap[5] = &J.tm[TM_R0];
         tmap[6] = &J.tm[TM_CODE];
-        x64n = J.x64[cur ^ 1];
+        x64n = (FF *)J.x64[cur ^ 1];
         t = (float *)J.t;
         r0 = (float *)J.r0;
         alpha = (float)sc.alpha;
         omega = (float)sc.omega;
         restart = sc.replace == 2;
     }
-    __device__ double iterate(const Geo &g, Shared &S, const Vals &a, const Pos &ps) const
+    __device__ FF iterate(const Geo &g, Shared &S, const Vals &a, const Pos &ps) const
     {
         const float inv = inv_of<float, true>(S, g, a.code, ps);
         const float ek = a.e + alpha * (a.p * inv) + omega * ((a.r - alpha * a.v) * inv);
-        return a.x + (double)ek;
+        return ff_add_f(a.x, ek);
     }
-    __device__ double field(const Geo &g, const Coef<double> &, Shared &S, const Vals &a, const Pos &ps) const
+    __device__ FF field(const Geo &g, const Coef<FF> &, Shared &S, const Vals &a, const Pos &ps) const
     {
         return iterate(g, S, a, ps);
     }
-    __device__ Own own(const Geo &g, const Coef<double> &, Shared &S, const Vals &a, const Pos &ps, double &f) const
+    __device__ Own own(const Geo &g, const Coef<FF> &, Shared &S, const Vals &a, const Pos &ps, FF &f) const
     {
         f = iterate(g, S, a, ps);
         return Own{a.code, a.r0};
     }
-    __device__ Out apply(const Geo &g, const Coef<double> &C, Shared &, const Own &o, const Pos &ps, double fc,
-                         double fxp, double fxm, double fyp, double fym, double fzp, double fzm)
+    __device__ Out apply(const Geo &g, const Coef<FF> &C, Shared &, const Own &o, const Pos &ps, FF fc, FF fxp,
+                         FF fxm, FF fyp, FF fym, FF fzp, FF fzm)
     {
-        const double d = diag_of<double, false>(C, g, o.code, ps);
-        const double ax = stencil7<double>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
-        const double b = rhs_at<double>(C, g, o.code, ps.x, ps.y, ps.z);
-        const float r32 = (float)(b - ax);
-        const float b32 = (float)b;
+        const FF ax = stencil7_ff(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag_ff(C, o.code, ps));
+        const FF b = rhs_at<FF>(C, g, o.code, ps.x, ps.y, ps.z);
+        const float r32 = ff_to_float(ff_add(b, ff_neg(ax)));
+        const float b32 = ff_to_float(b);
         a_rr.add_prod(r32, r32);
         a_bb.add_prod(b32, b32);
         a_d.add_prod(restart ? r32 : o.r0, r32);
@@ -252,7 +254,7 @@ struct OpReplaceBi2 {
     }
     __device__ void store(int64_t i, const Out &a, const Out &b, bool v0_, bool v1_)
     {
-        store2<double>(x64n, i, a.x, b.x, v0_, v1_);
+        store2<FF>(x64n, i, a.x, b.x, v0_, v1_);
         store2<float>(t, i, a.r, b.r, v0_, v1_);
         if (restart) store2<float>(r0, i, a.r, b.r, v0_, v1_);
     }
@@ -379,7 +381,7 @@ __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
     const Job &J = L.jobs[s_job];
     const TileCoords t = tile_coords(J, tid);
     const Geo g{J.nx, J.ny, J.nz, J.dir >> 1, (J.dir & 1) ? -1 : 1, J.pitch};
-    double *x64 = J.x64[0];
+    FF *x64 = (FF *)J.x64[0];
     float *e = (float *)J.x;
     // Two-sweep BiCGSTAB: the first replacement reads r, p, v (scaled by
     // alpha = omega = 0) and step 1 reads t; all start at zero.
@@ -388,7 +390,7 @@ __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
         if (!t.v[k]) continue;
         for (int z = t.z0; z < t.z1; ++z) {
             const int64_t i = g.idx(t.gx + k, t.gy, z);
-            x64[i] = (double)x0_at<float>(g, t.gx + k, t.gy, z);
+            x64[i] = FF(x0_at<float>(g, t.gx + k, t.gy, z), 0.f);
             e[i] = 0.f;
             if (zt) {
                 zr[i] = 0.f;
@@ -404,6 +406,26 @@ __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
 // D_cell * (c - c_next) / dx with c_next the neighbour one step along the
 // direction, or 0 with dx = 0.5 past the last plane.  D_cell is the float
 // coefficient of the voxel's phase.  Summed in FP64.
+template <typename TC>
+__device__ __forceinline__ double conc_at(const TC *c, int64_t i)
+{
+    if constexpr (std::is_same<TC, FF>::value) {
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(c) + i);
+        return (double)v.x + (double)v.y;
+    } else {
+        return (double)__ldg(c + i);
+    }
+}
+
+// The MIXED iterate as FP64 values (for the concentration output).
+__global__ void ff_to_double_kernel(const float2 *src, double *dst, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = src[i];
+        dst[i] = (double)v.x + (double)v.y;
+    }
+}
+
 template <typename TC>
 __global__ void __launch_bounds__(NTHREADS) tau_kernel(Launch L, int use_x64)
 {
@@ -427,10 +449,10 @@ __global__ void __launch_bounds__(NTHREADS) tau_kernel(Launch L, int use_x64)
         for (int z = t.z0; z < t.z1; ++z) {
             const int64_t i = g.idx(x, t.gy, z);
             const int kn = g.coord(x, t.gy, z) + g.sgn;
-            const double here = (double)__ldg(c + i);
+            const double here = conc_at(c, i);
             double prev = 0.0, rdx = 2.0;  // 1/dx: dx = 0.5 past the last plane
             if (kn >= 0 && kn < ext) {
-                prev = (double)__ldg(c + i + sstep);
+                prev = conc_at(c, i + sstep);
                 rdx = 1.0;
             }
             const int self = (__ldg(J.code + i) >> SELF_BIT) & 1;

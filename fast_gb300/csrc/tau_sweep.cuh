@@ -146,7 +146,11 @@ template <typename E, class SL, int S>
 __device__ __forceinline__ void sv2(const unsigned char *stage, const Pt &p, E &a, E &b)
 {
     const E *q = sp<E, SL, S>(stage, p);
-    if constexpr (sizeof(E) == 4) {
+    if constexpr (std::is_same<E, FF>::value) {
+        const float4 v = *reinterpret_cast<const float4 *>(q);
+        a = FF(v.x, v.y);
+        b = FF(v.z, v.w);
+    } else if constexpr (sizeof(E) == 4) {
         const float2 v = *reinterpret_cast<const float2 *>(q);
         a = v.x;
         b = v.y;
@@ -191,6 +195,17 @@ __host__ __device__ constexpr int sweep_dyn_smem()
 // thread pairs start at even columns; column 1 holds x0 - 1, column TX + 2
 // holds x0 + TX.
 constexpr int PW = TX + 4;
+
+// Type of an operation's per-thread partial sums: Op::R when it names one,
+// else its field type.
+template <class Op, class = void>
+struct RedType {
+    using type = typename Op::T;
+};
+template <class Op>
+struct RedType<Op, std::void_t<typename Op::R>> {
+    using type = typename Op::R;
+};
 
 // The sweep body, shared by the kernel entries below.
 template <class Op, int NSTAGE>
@@ -394,9 +409,10 @@ __device__ __forceinline__ void sweep_body(const Launch &L)
         op.store(i_col + plane * zs, r0, r1, v0, v1);
     }
 
-    T v[NV];
+    using RT = typename RedType<Op>::type;
+    RT v[NV];
     op.partials(v);
-    block_sum_store<NV, T>(v, J.part + local * NPART, s_red);
+    block_sum_store<NV, RT>(v, J.part + local * NPART, s_red);
     if (arrive_last(J.counter, J.ntiles, &s_flag)) {
         double tot[NV];
         sum_partials<NV>(J.part, J.ntiles, tot, s_red);

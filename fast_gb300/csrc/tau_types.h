@@ -7,12 +7,16 @@ namespace ft {
 
 // Tile of one thread block: TX x TY columns marching over ZC planes in z.
 // Each thread owns two neighbouring x columns (LANES), so a row of TX
-// voxels is TPR threads.
-constexpr int TX = 64;
-constexpr int TY = 8;
+// voxels is TPR threads; a block is always 256 threads (TX * TY = 512).
+#ifndef FAST_TAU_TX
+#define FAST_TAU_TX 64
+#endif
+constexpr int TX = FAST_TAU_TX;
 constexpr int LANES = 2;
 constexpr int TPR = TX / LANES;
+constexpr int TY = 256 / TPR;
 constexpr int NTHREADS = TPR * TY;
+static_assert(NTHREADS == 256 && TX % 16 == 0, "tile must be 256 threads, 16-element aligned in x");
 constexpr int HY = TY + 2;   // tile rows + one halo row on each side
 constexpr int NPART = 4;     // partial sums per block per kernel
 
@@ -99,7 +103,7 @@ struct Job {
     void *p[2];                  // search direction ping-pong (T)
     void *v[2];                  // BiCGSTAB v ping-pong (T)
     void *t;                     // MIXED BiCGSTAB: t = A s, kept from step 2 to step 1 (FP32)
-    double *x64[2];              // MIXED FP64 solution ping-pong
+    void *x64[2];                // MIXED extended-precision iterate ping-pong: float-float (hi, lo) pairs
     Scalars *sc;
     double *part;                // ntiles * NPART partial sums
     uint32_t *counter;           // finisher arrival counter
@@ -112,6 +116,11 @@ struct Job {
     float finv_b[7][128];        // 1/diag, FP32
     double ddiag_int[128];       // interior diagonal, FP64
     double dinv_int[128];        // 1/diag, FP64
+    // MIXED residual replacement: the FP64 values above as float-float
+    // pairs (value = hi + lo), the diagonal by (boundary count + 2, code).
+    float xdiag_hi[7][128], xdiag_lo[7][128];
+    float xface[2][2][2];        // [self solid][neighbour solid][hi, lo]
+    float xcell2[2][2];          // 2*D by solid bit, [hi, lo]
     float c_tau[2];              // tau cell coefficients (float coeffs of the reference)
     int32_t inner_parity;        // unused, keeps alignment
     int32_t pad0;
