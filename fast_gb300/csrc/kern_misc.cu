@@ -6,24 +6,42 @@ namespace ft {
 
 constexpr int kStages = 3;
 
+// The replacement slot runs at the head of every iteration and is idle in
+// most: its kernels walk the tiles with one resident wave of blocks
+// (sweep_kernel_tiles), sized here from the occupancy of each kernel.
+int g_resident_bi = 0, g_resident_cg = 0;
+
 void launch_replace(bool bicg, const Launch &L, cudaStream_t st)
 {
+    const int64_t resident = bicg ? g_resident_bi : g_resident_cg;
+    const unsigned grid = (unsigned)(L.nblocks < resident ? L.nblocks : resident);
     if (bicg)
-        sweep_kernel<OpReplaceBi2, kStages>
-            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpReplaceBi2, kStages>(), st>>>(L);
+        sweep_kernel_tiles<OpReplaceBi2, kStages>
+            <<<grid, NTHREADS, sweep_dyn_smem<OpReplaceBi2, kStages>(), st>>>(L);
     else
-        sweep_kernel<OpReplace<false>, kStages>
-            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpReplace<false>, kStages>(), st>>>(L);
+        sweep_kernel_tiles<OpReplace<false>, kStages>
+            <<<grid, NTHREADS, sweep_dyn_smem<OpReplace<false>, kStages>(), st>>>(L);
+}
+
+template <class Op>
+static cudaError_t configure_tiles(int &resident)
+{
+    cudaError_t e = cudaFuncSetAttribute(sweep_kernel_tiles<Op, kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         sweep_dyn_smem<Op, kStages>());
+    int per_sm = 0, dev = 0, sms = 0;
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel_tiles<Op, kStages>, NTHREADS,
+                                                          sweep_dyn_smem<Op, kStages>());
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    resident = (per_sm < 1 ? 1 : per_sm) * (sms < 1 ? 1 : sms);
+    return e;
 }
 
 cudaError_t configure_misc()
 {
-    cudaError_t a = cudaFuncSetAttribute(sweep_kernel<OpReplaceBi2, kStages>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         sweep_dyn_smem<OpReplaceBi2, kStages>());
-    cudaError_t b = cudaFuncSetAttribute(sweep_kernel<OpReplace<false>, kStages>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         sweep_dyn_smem<OpReplace<false>, kStages>());
+    cudaError_t a = configure_tiles<OpReplaceBi2>(g_resident_bi);
+    cudaError_t b = configure_tiles<OpReplace<false>>(g_resident_cg);
     return a != cudaSuccess ? a : b;
 }
 

@@ -207,9 +207,17 @@ struct RedType<Op, std::void_t<typename Op::R>> {
     using type = typename Op::R;
 };
 
-// The sweep body, shared by the kernel entries below.
+// The sweep of one tile `blk` (a block index of the launch), shared by the
+// kernel entries below.  `qb` counts the planes this block has taken through
+// its stage ring so far (ring slot and mbarrier phase continue from it), and
+// `ready` tells whether the block's mbarriers are initialised; both carry
+// over when one block sweeps several tiles.  Returns SWEEP_DONE, SWEEP_IDLE
+// (the tile's right-hand side is not active; *idle_end = its last tile + 1)
+// or SWEEP_FAULT.
+enum { SWEEP_DONE = 0, SWEEP_IDLE = 1, SWEEP_FAULT = 2 };
+
 template <class Op, int NSTAGE>
-__device__ __forceinline__ void sweep_body(const Launch &L)
+__device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb, bool &ready, int64_t *idle_end)
 {
     using T = typename Op::T;
     using SL = typename Op::SL;
@@ -225,19 +233,23 @@ __device__ __forceinline__ void sweep_body(const Launch &L)
     __shared__ typename Op::Shared S;
 
     const int tid = threadIdx.x;
+    __syncthreads();  // the previous tile of this block is done with the shared state
     if (tid == 0) {
-        s_job = find_job(L, (int64_t)blockIdx.x);
+        s_job = find_job(L, blk);
         s_go = Op::active(*L.jobs[s_job].sc) ? 1 : 0;
         s_err = 0;
     }
     __syncthreads();
-    if (!s_go) return;
+    if (!s_go) {
+        *idle_end = L.jobs[s_job].tile_base + L.jobs[s_job].ntiles;
+        return SWEEP_IDLE;
+    }
     const Job &J = L.jobs[s_job];
     load_coef<T>(C, J, tid);
     Op::load_shared(S, J, tid);
 
     const Geo g{J.nx, J.ny, J.nz, J.dir >> 1, (J.dir & 1) ? -1 : 1, J.pitch};
-    const int64_t local = (int64_t)blockIdx.x - J.tile_base;
+    const int64_t local = blk - J.tile_base;
     const int tx_t = (int)(local % J.tiles_x);
     const int ty_t = (int)((local / J.tiles_x) % J.tiles_y);
     const int tz_t = (int)(local / ((int64_t)J.tiles_x * J.tiles_y));
@@ -260,15 +272,17 @@ __device__ __forceinline__ void sweep_body(const Launch &L)
     const uint32_t stage0 = (raw0 + 127u) & ~127u;
     unsigned char *const sbase = dsm + (stage0 - raw0);
     if (tid == 0) {
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        if (!ready)
+            for (int s = 0; s < NSTAGE; ++s) mbar_init(smem_u32(&bars[s]), 1);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 #pragma unroll
         for (int s = 0; s < SL::N; ++s) prefetch_tmap(op.tmap[s]);
     }
+    ready = true;
     __syncthreads();
-    // Tile loads of plane pa+q into stage q % NSTAGE (thread 0 only).
+    // Tile loads of plane pa+q into ring slot (qb + q) % NSTAGE (thread 0 only).
     auto issue = [&](int q) {
-        const int st = q % NSTAGE;
+        const int st = (qb + q) % NSTAGE;
         const uint32_t bar = smem_u32(&bars[st]);
         mbar_arrive_expect_tx(bar, (uint32_t)SL::tx_bytes());
 #pragma unroll
@@ -314,17 +328,18 @@ __device__ __forceinline__ void sweep_body(const Launch &L)
     int q = 0;
     for (; q < NP; ++q) {
         const int zq = pa + q;
-        const int st = q % NSTAGE;
+        const int st = (qb + q) % NSTAGE;
+        const uint32_t par = (uint32_t)(((qb + q) / NSTAGE) & 1);
 #if FAST_TAU_WAIT_WARP0
         // Warp 0 waits for the stage; the other warps sleep in the barrier
         // instead of spinning on the mbarrier, then observe the completed
         // phase once.
-        if (tid < 32 && !mbar_wait_bounded(smem_u32(&bars[st]), (uint32_t)((q / NSTAGE) & 1))) s_err = 1;
+        if (tid < 32 && !mbar_wait_bounded(smem_u32(&bars[st]), par)) s_err = 1;
         __syncthreads();
         if (s_err) break;
-        if (tid >= 32) (void)mbar_try_wait(smem_u32(&bars[st]), (uint32_t)((q / NSTAGE) & 1));
+        if (tid >= 32) (void)mbar_try_wait(smem_u32(&bars[st]), par);
 #else
-        if (!mbar_wait_bounded(smem_u32(&bars[st]), (uint32_t)((q / NSTAGE) & 1))) s_err = 1;
+        if (!mbar_wait_bounded(smem_u32(&bars[st]), par)) s_err = 1;
 #endif
         const unsigned char *stage = sbase + st * SB;
         const bool out_plane = zq >= z0 && zq < z1;
@@ -389,11 +404,12 @@ __device__ __forceinline__ void sweep_body(const Launch &L)
         if (tid == 0) {
             const int issued = min(q + NSTAGE, NP);
             for (int k = q; k < issued; ++k)
-                mbar_wait_bounded(smem_u32(&bars[k % NSTAGE]), (uint32_t)((k / NSTAGE) & 1));
+                mbar_wait_bounded(smem_u32(&bars[(qb + k) % NSTAGE]), (uint32_t)(((qb + k) / NSTAGE) & 1));
             atomicExch(&J.sc->state, (int32_t)FAULT);
         }
-        return;
+        return SWEEP_FAULT;
     }
+    qb += NP;
     // The last plane of the volume has no z+1 neighbour: apply it here.
     if (pb == z1 - 1 && (v0 || v1)) {
         const int zs = z1 - 1;
@@ -422,20 +438,50 @@ __device__ __forceinline__ void sweep_body(const Launch &L)
             *J.counter = 0u;
         }
     }
+    return SWEEP_DONE;
 }
 
-// Kernel entries: the compiler's own register choice, or (for an operation
-// that is otherwise held to two blocks per SM) a bound that fits MB blocks.
+// Kernel entries: one tile per block with the compiler's own register
+// choice, or (for an operation that is otherwise held to two blocks per SM)
+// a bound that fits MB blocks.
 template <class Op, int NSTAGE>
 __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
 {
-    sweep_body<Op, NSTAGE>(L);
+    int qb = 0;
+    bool ready = false;
+    int64_t idle_end;
+    sweep_body<Op, NSTAGE>(L, (int64_t)blockIdx.x, qb, ready, &idle_end);
 }
 
 template <class Op, int NSTAGE, int MB>
 __global__ void __launch_bounds__(NTHREADS, MB) sweep_kernel_mb(Launch L)
 {
-    sweep_body<Op, NSTAGE>(L);
+    int qb = 0;
+    bool ready = false;
+    int64_t idle_end;
+    sweep_body<Op, NSTAGE>(L, (int64_t)blockIdx.x, qb, ready, &idle_end);
+}
+
+// A resident grid that walks the launch's tiles (tile = blockIdx.x +
+// k * gridDim.x) and skips the rest of a right-hand side it finds inactive:
+// for operations that most launches leave idle (the residual replacement
+// slot of every iteration), so an idle launch costs one wave of blocks.
+template <class Op, int NSTAGE>
+__global__ void __launch_bounds__(NTHREADS) sweep_kernel_tiles(Launch L)
+{
+    int qb = 0;
+    bool ready = false;
+    for (int64_t blk = blockIdx.x; blk < L.nblocks;) {
+        int64_t idle_end = 0;
+        const int r = sweep_body<Op, NSTAGE>(L, blk, qb, ready, &idle_end);
+        if (r == SWEEP_FAULT) return;
+        if (r == SWEEP_IDLE && idle_end > blk + gridDim.x) {
+            // first tile >= idle_end that belongs to this block
+            blk += ((idle_end - blk + gridDim.x - 1) / gridDim.x) * gridDim.x;
+        } else {
+            blk += gridDim.x;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
