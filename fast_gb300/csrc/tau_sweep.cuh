@@ -41,16 +41,31 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t byt
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
+// HINT > 0: the wait may suspend the thread for up to HINT ns while the
+// phase is incomplete (a suspended thread issues nothing) instead of
+// returning at once to the polling loop.  Which is better depends on the
+// kernel (an operation names its hint as wait_hint_ns; default 0).
+template <uint32_t HINT = 0>
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
 {
     uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
+    if constexpr (HINT > 0) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity), "r"(HINT)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+    }
     return ok != 0;
 }
 
@@ -64,15 +79,30 @@ __device__ __forceinline__ uint64_t global_timer_ns()
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 
 // Waits for phase `parity` of the mbarrier, giving up after kWaitLimitNs.
+template <uint32_t HINT = 0>
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
 {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait<HINT>(bar, parity)) return true;
     const uint64_t t0 = global_timer_ns();
-    while (!mbar_try_wait(bar, parity)) {
+    while (!mbar_try_wait<HINT>(bar, parity)) {
         if (global_timer_ns() - t0 > kWaitLimitNs) return false;
     }
     return true;
 }
+
+#ifndef FAST_TAU_HINT_CG
+#define FAST_TAU_HINT_CG 0
+#endif
+
+// An operation's wait hint: Op::wait_hint_ns when it names one, else 0.
+template <class Op, class = void>
+struct WaitHint {
+    static constexpr uint32_t ns = 0;
+};
+template <class Op>
+struct WaitHint<Op, std::void_t<decltype(Op::wait_hint_ns)>> {
+    static constexpr uint32_t ns = Op::wait_hint_ns;
+};
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *tm, int x, int y, int z, uint32_t bar)
 {
@@ -339,7 +369,7 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         if (s_err) break;
         if (tid >= 32) (void)mbar_try_wait(smem_u32(&bars[st]), par);
 #else
-        if (!mbar_wait_bounded(smem_u32(&bars[st]), par)) s_err = 1;
+        if (!mbar_wait_bounded<WaitHint<Op>::ns>(smem_u32(&bars[st]), par)) s_err = 1;
 #endif
         const unsigned char *stage = sbase + st * SB;
         const bool out_plane = zq >= z0 && zq < z1;
@@ -670,6 +700,7 @@ template <typename TT, typename ST>
 struct OpCG1 {
     using T = TT;
     static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
+    static constexpr uint32_t wait_hint_ns = FB ? FAST_TAU_HINT_CG : 0;
     using SL = Streams<sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 1;
     using Shared = NoShared;
@@ -748,6 +779,7 @@ template <typename TT, typename ST>
 struct OpCG2 {
     using T = TT;
     static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
+    static constexpr uint32_t wait_hint_ns = FB ? FAST_TAU_HINT_CG : 0;
     using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 2;
     using Shared = NoShared;
@@ -1221,9 +1253,17 @@ __device__ __forceinline__ void bicg2_k2_finish(Scalars &sc, double ts, double t
     sc.beta = (rho_new / rho_old) * (sc.alpha / omega);
 }
 
+#ifndef FAST_TAU_HINT_K1
+#define FAST_TAU_HINT_K1 20000
+#endif
+#ifndef FAST_TAU_HINT_K2
+#define FAST_TAU_HINT_K2 0
+#endif
+
 struct OpBiK1 {
     using T = float;
     static constexpr bool FB = true;
+    static constexpr uint32_t wait_hint_ns = FAST_TAU_HINT_K1;
     using SL = Streams<4, 4, 4, 4, 4, 4, 1>;  // r, v, t, p, e, r0, code
     static constexpr int NV = 2;
     using Shared = NoShared;
@@ -1320,6 +1360,7 @@ struct OpBiK1 {
 struct OpBiK2 {
     using T = float;
     static constexpr bool FB = true;
+    static constexpr uint32_t wait_hint_ns = FAST_TAU_HINT_K2;
     using SL = Streams<4, 4, 4, 1>;  // r, v, r0, code
     static constexpr int NV = 4;
     using Shared = NoShared;
