@@ -55,6 +55,16 @@ struct Coef {
     T inv_b[NB][128];  // its reciprocal
 };
 
+// FP32: the diagonal and its inverse interleaved, {diag, 1/diag}, so that
+// a voxel that needs both reads one 8-byte entry.
+template <>
+struct Coef<float> {
+    static constexpr int NB = NBC;
+    float face[2][2];
+    float cell2[2];
+    float2 di[NBC][128];  // {diag, 1/diag} by (boundary count + 2, code)
+};
+
 template <typename T>
 __device__ __forceinline__ void load_coef(Coef<T> &C, const Job &J, int tid)
 {
@@ -66,10 +76,8 @@ __device__ __forceinline__ void load_coef(Coef<T> &C, const Job &J, int tid)
         if (tid < 4) C.face[tid >> 1][tid & 1] = J.dface[tid >> 1][tid & 1];
         if (tid < 2) C.cell2[tid] = 2.0 * J.dcell[tid];
     } else {
-        for (int k = tid; k < NBC * 128; k += NTHREADS) {
-            C.diag_b[k >> 7][k & 127] = J.fdiag_b[k >> 7][k & 127];
-            C.inv_b[k >> 7][k & 127] = J.finv_b[k >> 7][k & 127];
-        }
+        for (int k = tid; k < NBC * 128; k += NTHREADS)
+            C.di[k >> 7][k & 127] = make_float2(J.fdiag_b[k >> 7][k & 127], J.finv_b[k >> 7][k & 127]);
         if (tid < 4) C.face[tid >> 1][tid & 1] = J.fface[tid >> 1][tid & 1];
         if (tid < 2) C.cell2[tid] = (float)(2.0 * J.dcell[tid]);
     }
@@ -181,14 +189,69 @@ __device__ __forceinline__ T diag_general(const Coef<T> &C, const Geo &g, uint32
 template <typename T>
 __host__ __device__ constexpr int interior_row() { return Coef<T>::NB == 1 ? 0 : 2; }
 
+// Interior entries of the tables: row `row` (FP32 boundary-count row, or
+// the single FP64 row), diagonal and inverse.
+template <typename T>
+__device__ __forceinline__ T tab_diag(const Coef<T> &C, int row, uint32_t code)
+{
+    if constexpr (std::is_same<T, float>::value) return C.di[row][code & 127].x;
+    else return C.diag_b[row][code & 127];
+}
+
+template <typename T>
+__device__ __forceinline__ T tab_inv(const Coef<T> &C, int row, uint32_t code)
+{
+    if constexpr (std::is_same<T, float>::value) return C.di[row][code & 127].y;
+    else return C.inv_b[row][code & 127];
+}
+
 template <typename T, bool FAST>
 __device__ __forceinline__ T diag_of(const Coef<T> &C, const Geo &g, uint32_t code, const Pos &p)
 {
     if constexpr (FAST) {
-        return C.diag_b[p.bc + 2][code & 127];
+        return tab_diag(C, p.bc + 2, code);
     } else {
         if (code & (1u << BND_BIT)) return diag_general(C, g, code, p.x, p.y, p.z);
-        return C.diag_b[interior_row<T>()][code & 127];
+        return tab_diag(C, interior_row<T>(), code);
+    }
+}
+
+// {diagonal, inverse} of the voxel at p (FP32).
+template <bool FAST>
+__device__ __forceinline__ float2 dinv_of(const Coef<float> &C, const Geo &g, uint32_t code, const Pos &p);
+
+// The diagonal and its inverse together: one table entry in FP32.
+template <typename T, bool FAST>
+__device__ __forceinline__ void diag_inv(const Coef<T> &C, const Geo &g, uint32_t code, const Pos &p, T &d, T &inv);
+
+// {diagonal, inverse} of the voxel at p (FP32).
+template <bool FAST>
+__device__ __forceinline__ float2 dinv_of(const Coef<float> &C, const Geo &g, uint32_t code, const Pos &p)
+{
+    if constexpr (FAST) {
+        return C.di[p.bc + 2][code & 127];
+    } else {
+        if (code & (1u << BND_BIT)) {
+            const float d = diag_general(C, g, code, p.x, p.y, p.z);
+            return make_float2(d, 1.0f / d);
+        }
+        return C.di[interior_row<float>()][code & 127];
+    }
+}
+
+template <typename T, bool FAST>
+__device__ __forceinline__ T inv_from_diag(const Coef<T> &C, uint32_t code, const Pos &p, T d);
+
+template <typename T, bool FAST>
+__device__ __forceinline__ void diag_inv(const Coef<T> &C, const Geo &g, uint32_t code, const Pos &p, T &d, T &inv)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        const float2 di = dinv_of<FAST>(C, g, code, p);
+        d = di.x;
+        inv = di.y;
+    } else {
+        d = diag_of<T, FAST>(C, g, code, p);
+        inv = inv_from_diag<T, FAST>(C, code, p, d);
     }
 }
 
@@ -196,10 +259,10 @@ template <typename T, bool FAST>
 __device__ __forceinline__ T inv_of(const Coef<T> &C, const Geo &g, uint32_t code, const Pos &p)
 {
     if constexpr (FAST) {
-        return C.inv_b[p.bc + 2][code & 127];
+        return tab_inv(C, p.bc + 2, code);
     } else {
         if (code & (1u << BND_BIT)) return T(1) / diag_general(C, g, code, p.x, p.y, p.z);
-        return C.inv_b[interior_row<T>()][code & 127];
+        return tab_inv(C, interior_row<T>(), code);
     }
 }
 
@@ -208,9 +271,9 @@ template <typename T, bool FAST>
 __device__ __forceinline__ T inv_from_diag(const Coef<T> &C, uint32_t code, const Pos &p, T d)
 {
     if constexpr (FAST) {
-        return C.inv_b[p.bc + 2][code & 127];
+        return tab_inv(C, p.bc + 2, code);
     } else {
-        return (code & (1u << BND_BIT)) ? T(1) / d : C.inv_b[interior_row<T>()][code & 127];
+        return (code & (1u << BND_BIT)) ? T(1) / d : tab_inv(C, interior_row<T>(), code);
     }
 }
 

@@ -705,7 +705,7 @@ struct OpCG1 {
     static constexpr int NV = 1;
     using Shared = NoShared;
     struct Vals { T r, p; uint32_t code; };
-    struct Own { uint32_t code; };
+    struct Own { uint32_t code; T d; };
     struct Out { T p; };
     const CUtensorMap *tmap[SL::N];
     Faces<T> F;
@@ -744,16 +744,17 @@ struct OpCG1 {
         const T zi = v.r * inv_of<T, FB>(C, g, v.code, ps);
         return v.p * beta + zi;  // __aAddAlphaBKernel: p = p*beta + z
     }
-    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &S, const Vals &v, const Pos &ps, T &f) const
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps, T &f) const
     {
-        f = field(g, C, S, v, ps);
-        return Own{v.code};
+        T d, inv;
+        diag_inv<T, FB>(C, g, v.code, ps, d, inv);
+        f = v.p * beta + v.r * inv;  // as field()
+        return Own{v.code, d};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc,
+    __device__ Out apply(const Geo &, const Coef<T> &, Shared &, const Own &o, const Pos &, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_of<T, FB>(C, g, o.code, ps);
-        const T q = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T q = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, o.d);
         pap.add_prod(fc, q);
         return Out{fc};
     }
@@ -823,11 +824,11 @@ struct OpCG2 {
     __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
-        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        T d, inv;
+        diag_inv<T, FB>(C, g, o.code, ps, d, inv);
         const T q = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         const T xn = o.x + alpha * fc;        // __aAddBetaBKernel(x, p, alpha)
         const T rn = o.r + (-alpha) * q;      // __aAddBetaBKernel(r, ap, -alpha)
-        const T inv = inv_from_diag<T, FB>(C, o.code, ps, d);
         rr.add_prod(rn, rn);
         rz.add_prod(rn, rn * inv);
         return Out{xn, rn};
