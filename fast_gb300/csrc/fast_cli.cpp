@@ -4,6 +4,8 @@
 // CSVOutputModule.h:35-112), over libfasttau.so's C ABI.
 //
 //   fast alpha <input.bin|tiff folder> [-d ...] [--basic] [crops] [-o out.csv]
+//   fast slice <input.bin|tiff folder> [--size x[,y,z]] [--stride ..] [--begin ..]
+//              [--end ..] [--out folder] [crops]
 //
 // alpha rows (AlphaModule::getAlpha, AlphaModule.h:28-179): without --basic,
 // one row per direction with the area of the pore space connected to that
@@ -12,6 +14,16 @@
 // carrying the whole area (radBasic, radBasicTime) and no dir column.
 // Columns are sorted by name as the reference's row map sorts them.  --mesh
 // (OBJ export) and --segmentinfo are not provided.
+//
+// slice rows (SliceModule.h:34-240): every sub-volume of --size at origins
+// begin, begin + stride, ... with origin + size <= end (end defaults to the
+// last voxel index, as the reference) is saved as <out>/<stem>/XXXX_YYYY_ZZZZ.bin
+// and gets one row per positive direction in <out>/data.csv: ID (that path
+// below <out>), alpha (the basic reactive area), porosity, tau (FP32 CG,
+// tol 1e-5, 10000 iterations), sizex..z, originx..z, dir.  The reference
+// solves the sub-volumes one at a time (small ones with its CPU solver);
+// here all of them go through the batched GPU solver, up to 340 sub-volumes
+// (1020 right-hand sides) per launch.
 //
 //   fast tau <input.bin|tiff folder> [-d x|y|z|xy..|all|pos|neg|xneg|yneg|zneg]
 //            [--solver CG|BICGSTAB] [--tol N] [--iter N] [-p d|f|mixed]
@@ -36,6 +48,8 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <array>
+#include <cerrno>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -67,7 +81,9 @@ int usage(const char *why)
                  "                [--iter N] [-p d|f|mixed] [--sub x,y,z] [--origin x,y,z] [--randsub x,y,z]\n"
                  "                [--aspect x,y,z] [-o out.csv] [-v] [--cpu] [-j N]\n"
                  "       fast alpha <input.bin|tiff folder> [-d x|y|z|all|pos|neg] [--basic] [--sub x,y,z]\n"
-                 "                [--origin x,y,z] [--randsub x,y,z] [--aspect x,y,z] [-o out.csv]\n";
+                 "                [--origin x,y,z] [--randsub x,y,z] [--aspect x,y,z] [-o out.csv]\n"
+                 "       fast slice <input.bin|tiff folder> [--size x,y,z] [--stride x,y,z] [--begin x,y,z]\n"
+                 "                [--end x,y,z] [--out folder]\n";
     return why ? 1 : 0;
 }
 
@@ -333,6 +349,140 @@ int run_alpha(const std::string &name, const Vol &vol, const std::vector<int32_t
     return 0;
 }
 
+// mkdir -p
+bool make_dirs(const std::string &path)
+{
+    std::string cur;
+    std::stringstream ss(path);
+    std::string part;
+    if (!path.empty() && path[0] == '/') cur = "/";
+    while (std::getline(ss, part, '/')) {
+        if (part.empty()) continue;
+        cur += part + "/";
+        if (mkdir(cur.c_str(), 0755) != 0 && errno != EEXIST) return false;
+    }
+    return true;
+}
+
+// saveVolumeBinary (VolumeIO.cpp:256-277) of a uchar volume.
+bool save_bin(const std::string &path, const Vol &v)
+{
+    std::ofstream f(path, std::ios::binary);
+    if (!f.good()) return false;
+    const int32_t type = kTypeUchar, dim[3] = {(int32_t)v.nx, (int32_t)v.ny, (int32_t)v.nz};
+    const char flag = 0;
+    f.write((const char *)&type, 4);
+    f.write((const char *)dim, 12);
+    f.write(&flag, 1);
+    f.write((const char *)v.data.data(), (std::streamsize)v.data.size());
+    return f.good();
+}
+
+// SliceModule::execute (SliceModule.h:34-240), without its PER_SLICE PNG
+// branch (compiled out in the reference).
+int run_slice(const std::string &name, const Vol &vol, const int64_t size[3], const int64_t stride[3],
+              const int64_t begin_arg[3], const int64_t end_arg[3], const std::string &out_dir)
+{
+    const int64_t dim[3] = {vol.nx, vol.ny, vol.nz};
+    int64_t begin[3], end[3];
+    for (int k = 0; k < 3; k++) {
+        begin[k] = std::min(begin_arg[k], dim[k] - 1);
+        end[k] = std::max(end_arg[k], (int64_t)0);
+        if (end[k] == 0) end[k] = dim[k] - 1;
+        if (size[k] <= 0 || stride[k] <= 0) {
+            std::cerr << "error: --size and --stride must be positive\n";
+            return 1;
+        }
+    }
+    // stem: the last component of the input name (explode on '/')
+    std::string stem = name;
+    {
+        std::stringstream ss(name);
+        std::string part;
+        while (std::getline(ss, part, '/')) stem = part;
+    }
+    std::vector<std::array<int64_t, 3>> origins;
+    for (int64_t x0 = begin[0]; x0 + size[0] <= end[0]; x0 += stride[0])
+        for (int64_t y0 = begin[1]; y0 + size[1] <= end[1]; y0 += stride[1])
+            for (int64_t z0 = begin[2]; z0 + size[2] <= end[2]; z0 += stride[2]) origins.push_back({x0, y0, z0});
+    std::cout << "Subvolume count " << origins.size() << std::endl;
+    if (origins.empty()) {
+        std::cout << "Volume is not big enough " << dim[0] << ", " << dim[1] << ", " << dim[2] << ", need " << size[0]
+                  << ", " << size[1] << ", " << size[2] << std::endl;
+        return 0;
+    }
+    const std::string vol_dir = out_dir + "/" + stem;
+    if (!make_dirs(vol_dir)) {
+        std::cerr << "error: cannot create " << vol_dir << "\n";
+        return 1;
+    }
+    const std::string csv = out_dir + "/data.csv";
+    const int32_t dirs[3] = {FAST_X_POS, FAST_Y_POS, FAST_Z_POS};
+    fast_tau_params p;
+    fast_tau_params_init(&p);
+    p.solver = FAST_SOLVER_CG;
+    p.precision = FAST_PREC_F32;
+    p.tolerance = std::pow(10.0, -5);
+    p.max_iter = 10000;
+    p.porosity = -1.0;  // each sub-volume's own (getPorosity, float)
+    bool first_stdout = true;
+    const size_t kChunk = 340;  // 3 right-hand sides each, within one launch's 1024
+    for (size_t c0 = 0; c0 < origins.size(); c0 += kChunk) {
+        const size_t c1 = std::min(origins.size(), c0 + kChunk);
+        std::vector<Vol> subs(c1 - c0);
+        std::vector<fast_tau_volume> tv;
+        std::vector<double> alpha(c1 - c0), phi(c1 - c0);
+        std::vector<std::string> ids(c1 - c0);
+        for (size_t s = c0; s < c1; s++) {
+            Vol &sv = subs[s - c0];
+            sv = crop(vol, origins[s].data(), size);
+            char buf[64];
+            snprintf(buf, sizeof(buf), "%04lld_%04lld_%04lld.bin", (long long)origins[s][0], (long long)origins[s][1],
+                     (long long)origins[s][2]);
+            const std::string path = vol_dir + "/" + buf;
+            ids[s - c0] = path.substr(out_dir.size() + 1);
+            if (!save_bin(path, sv)) {
+                std::cerr << "error: cannot write " << path << "\n";
+                return 1;
+            }
+            // AlphaModule::getAlpha(subvolume, name, basic = true, {X_POS}):
+            // porosity as float, radBasic as float.
+            double ph = 0.0, area = 0.0;
+            if (fast_porosity(sv.data.data(), sv.nx, sv.ny, sv.nz, &ph, nullptr) != FAST_OK ||
+                fast_reactive_area(sv.data.data(), sv.nx, sv.ny, sv.nz, 0.5f, &area) != FAST_OK) {
+                std::cerr << "error: " << fast_last_error() << "\n";
+                return 1;
+            }
+            phi[s - c0] = ph;
+            alpha[s - c0] = area;
+            for (int32_t d : dirs) tv.push_back(fast_tau_volume{sv.data.data(), sv.nx, sv.ny, sv.nz, d, 0});
+        }
+        std::vector<fast_tau_result> res(tv.size());
+        const int st = fast_tau_solve_batch(tv.data(), (int32_t)tv.size(), &p, res.data());
+        if (st == FAST_CUDA_ERROR || st == FAST_NOMEM || st == FAST_TIMEOUT || st == FAST_BAD_ARG) {
+            std::cerr << "error: " << fast_last_error() << "\n";
+            return 1;
+        }
+        for (size_t s = c0; s < c1; s++) {
+            for (int k = 0; k < 3; k++) {
+                const fast_tau_result &r = res[(s - c0) * 3 + k];
+                std::vector<std::pair<std::string, std::string>> row = {
+                    {"ID", ids[s - c0]},
+                    {"alpha", fmt((float)alpha[s - c0])},
+                    {"porosity", fmt((float)phi[s - c0])},
+                    {"tau", fmt(r.status == FAST_OK ? r.tau : 0.0)},
+                    {"sizex", fmt(size[0])}, {"sizey", fmt(size[1])}, {"sizez", fmt(size[2])},
+                    {"originx", fmt(origins[s][0])}, {"originy", fmt(origins[s][1])},
+                    {"originz", fmt(origins[s][2])},
+                    {"dir", dir_string(dirs[k])}};
+                write_map_row(csv, first_stdout, row);
+            }
+        }
+    }
+    std::cout << "Generated " << origins.size() << " subvolumes" << std::endl;
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -340,8 +490,12 @@ int main(int argc, char **argv)
     if (argc < 2) return usage("missing action");
     const std::string action = argv[1];
     if (action == "-h" || action == "--help") return usage(nullptr);
-    if (action != "tau" && action != "alpha") return usage("only the `tau` and `alpha` actions are built");
+    if (action != "tau" && action != "alpha" && action != "slice")
+        return usage("only the `tau`, `alpha` and `slice` actions are built");
     bool basic = false;
+    int64_t slice_size[3] = {32, 32, 32}, slice_stride[3] = {1, 1, 1}, slice_begin[3] = {0, 0, 0},
+            slice_end[3] = {0, 0, 0};
+    std::string slice_out = "out";
 
     std::string input, dir = "x-", solver = "CG", precision = "double", out_path;
     int tol_exp = 6;
@@ -368,6 +522,11 @@ int main(int argc, char **argv)
         else if (a == "-v" || a == "--verbose") verbose = true;
         else if (a == "--cpu" || a == "--over" || a == "--oversubscribe") { /* accepted, no effect */ }
         else if (a == "--basic" && action == "alpha") basic = true;
+        else if (a == "--size" && action == "slice") parse3(next("--size"), slice_size);
+        else if (a == "--stride" && action == "slice") parse3(next("--stride"), slice_stride);
+        else if (a == "--begin" && action == "slice") parse3(next("--begin"), slice_begin);
+        else if (a == "--end" && action == "slice") parse3(next("--end"), slice_end);
+        else if (a == "--out" && action == "slice") slice_out = next("--out");
         else if ((a == "--mesh" || a == "--segmentinfo") && action == "alpha") {
             std::cerr << "error: " << a << " is not provided\n";
             return 1;
@@ -440,6 +599,7 @@ int main(int argc, char **argv)
     }
 
     if (action == "alpha") return run_alpha(input, vol, get_dirs(dir), basic, out_path);
+    if (action == "slice") return run_slice(input, vol, slice_size, slice_stride, slice_begin, slice_end, slice_out);
 
     fast_tau_params p;
     fast_tau_params_init(&p);

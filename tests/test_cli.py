@@ -117,3 +117,56 @@ def test_cli_crop_and_stdout(gpu, cli, tmp_path):
                                                      porosity_precomputed=True),
                             ft.DSOLVER_CG)
     assert abs(float(x["tau"]) - tau) <= 1e-5 * tau
+
+
+def test_slice_enumeration_without_gpu(cli, tmp_path):
+    # SliceModule.h:66-96: origins stop before origin + size exceeds end, and
+    # end defaults to the last voxel index -- a 20^3 volume holds no 20^3
+    # sub-volume.  Nothing reaches the GPU on this path.
+    m = np.zeros((20, 20, 20), np.uint8)
+    p = str(tmp_path / "v.bin")
+    volume_io.save_volume_binary(p, m)
+    r = run(cli, "slice", p, "--size", "20", "--out", str(tmp_path / "o"))
+    assert r.returncode == 0, r.stderr
+    assert "Subvolume count 0" in r.stdout and "not big enough" in r.stdout
+    r = run(cli, "slice", p, "--size", "0", "--out", str(tmp_path / "o"))
+    assert r.returncode == 1
+
+
+@pytest.mark.gpu
+def test_slice_rows(gpu, cli, oracle, tmp_path):
+    import ctypes as C
+    import fast_gb300 as ft
+    nx, ny, nz = 40, 36, 44
+    m = np.empty((nz, ny, nx), np.uint8)
+    assert gpu.fast_gen_spheres(m.ctypes.data_as(C.c_void_p), nx, ny, nz, 3, 2.0, 4.0, 0.5) == 0
+    p = str(tmp_path / "vol.bin")
+    volume_io.save_volume_binary(p, m)
+    out = tmp_path / "o"
+    r = run(cli, "slice", p, "--size", "16", "--stride", "12,10,14", "--out", str(out))
+    assert r.returncode == 0, r.stderr
+    xs = [x for x in range(0, nx) if x + 16 <= nx - 1][::1]
+    origins = [(x, y, z) for x in range(0, nx - 16, 12) for y in range(0, ny - 16, 10) for z in range(0, nz - 16, 14)
+               if x + 16 <= nx - 1 and y + 16 <= ny - 1 and z + 16 <= nz - 1]
+    assert xs and f"Subvolume count {len(origins)}" in r.stdout
+    with open(out / "data.csv") as f:
+        header = f.readline().strip().split(",")
+    assert header == ["ID", "alpha", "dir", "originx", "originy", "originz", "porosity", "sizex", "sizey", "sizez",
+                      "tau"]
+    rows = list(csv.DictReader(open(out / "data.csv")))
+    assert len(rows) == 3 * len(origins)
+    for k, (x, y, z) in enumerate(origins):
+        sub = np.ascontiguousarray(m[z:z + 16, y:y + 16, x:x + 16])
+        name = f"vol.bin/{x:04d}_{y:04d}_{z:04d}.bin"
+        saved = volume_io.load_volume_binary(str(out / name)).data
+        np.testing.assert_array_equal(saved, sub)
+        phi = float(np.float32((sub == 0).sum() / sub.size))
+        for d, dname in enumerate(["X_POS", "Y_POS", "Z_POS"]):
+            row = rows[3 * k + d]
+            assert row["ID"] == name and row["dir"] == dname
+            assert (int(row["originx"]), int(row["originy"]), int(row["originz"])) == (x, y, z)
+            assert float(row["porosity"]) == pytest.approx(phi, rel=1e-5)
+            ref = oracle.get_tortuosity(sub, dir=2 * d, tol=1e-10)
+            if ref["status"] == 0 and ref["tau"] > 0:
+                assert float(row["tau"]) == pytest.approx(ref["tau"], rel=1e-3)
+        assert float(rows[3 * k]["alpha"]) == pytest.approx(oracle.reactive_area(sub), rel=1e-5)
