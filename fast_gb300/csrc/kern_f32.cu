@@ -19,6 +19,14 @@ constexpr int kStages = FAST_TAU_STAGES_F32;
 // own choice and a 4-stage ring fit two; measured 389 against 416 us per
 // launch on the 256^3 x 3 workload).
 constexpr int kStagesK1 = FAST_TAU_STAGES_K1;
+#ifndef FAST_TAU_STAGES_CGF
+#define FAST_TAU_STAGES_CGF 3
+#endif
+#ifndef FAST_TAU_BLOCKS_CGF
+#define FAST_TAU_BLOCKS_CGF 2
+#endif
+constexpr int kStagesCGF = FAST_TAU_STAGES_CGF;
+constexpr int kBlocksCGF = FAST_TAU_BLOCKS_CGF;
 constexpr int kBlocksK1 = 3;
 
 template <class Op, int NS = kStages>
@@ -75,8 +83,12 @@ cudaError_t configure_f32()
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          sweep_dyn_smem<OpBiK1, kStagesK1>());
     cudaError_t d = cfg<OpBiK2>();
+    cudaError_t f = cudaFuncSetAttribute(sweep_kernel_mb<OpCGF, kStagesCGF, kBlocksCGF>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         sweep_dyn_smem<OpCGF, kStagesCGF>());
     if (a != cudaSuccess) return a;
     if (b != cudaSuccess) return b;
+    if (f != cudaSuccess) return f;
     return c != cudaSuccess ? c : d;
 }
 
@@ -87,6 +99,9 @@ void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st)
         sweep_kernel_mb<OpBiK1, kStagesK1, kBlocksK1>
             <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpBiK1, kStagesK1>(), st>>>(L);
     else if (s == Step::BI_K2) go<OpBiK2>(L, st);
+    else if (s == Step::CG_F)
+        sweep_kernel_mb<OpCGF, kStagesCGF, kBlocksCGF>
+            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpCGF, kStagesCGF>(), st>>>(L);
     else dispatch<double>(s, L, st);
 }
 

@@ -114,7 +114,7 @@ int steps_of(const Ctx &C, int solver, std::vector<Step> &steps)
 {
     const bool mixed = C.cfg.precision == FAST_PREC_MIXED;
     if (solver == FAST_SOLVER_CG) {
-        steps = mixed ? std::vector<Step>{Step::REPLACE_CG, Step::CG1, Step::CG2} : std::vector<Step>{Step::CG1, Step::CG2};
+        steps = mixed ? mixed_steps(FAST_SOLVER_CG) : std::vector<Step>{Step::CG1, Step::CG2};
     } else {
         steps = mixed ? std::vector<Step>{Step::REPLACE_BI, Step::BI_K1, Step::BI_K2}
                       : std::vector<Step>{Step::BI_RESTART, Step::BI1, Step::BI2, Step::BI3};

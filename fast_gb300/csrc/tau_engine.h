@@ -74,5 +74,9 @@ int status_of(int state);
 int check_params(const fast_tau_params *p);
 int check_volume(const void *mask, int64_t nx, int64_t ny, int64_t nz);
 void dispatch_mixed(Step s, const Launch &L, cudaStream_t st);
+// The per-iteration steps of a MIXED solve (CG: one fused sweep, or the
+// classic two with FAST_TAU_CG_FUSED=0).
+bool cg_fused_enabled();
+std::vector<Step> mixed_steps(int solver);
 
 }  // namespace ft

@@ -156,6 +156,7 @@ int kind_of(Step s)
     case Step::REPLACE_BI: return FAST_K_REPLACE;
     case Step::BI_K1: return FAST_K_BI1;
     case Step::BI_K2: return FAST_K_BI2;
+    case Step::CG_F: return FAST_K_CGF;
     }
     return FAST_K_COUNT - 1;
 }
@@ -383,6 +384,14 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
 
 void dispatch_f64(Step s, const Launch &L, cudaStream_t st) { launch_pure_f64(s, L, st); }
 void dispatch_f32(Step s, const Launch &L, cudaStream_t st) { launch_pure_f32(s, L, st); }
+std::vector<Step> mixed_steps(int solver)
+{
+    if (solver == FAST_SOLVER_CG)
+        return cg_fused_enabled() ? std::vector<Step>{Step::REPLACE_CG, Step::CG_F}
+                                  : std::vector<Step>{Step::REPLACE_CG, Step::CG1, Step::CG2};
+    return {Step::REPLACE_BI, Step::BI_K1, Step::BI_K2};
+}
+
 void dispatch_mixed(Step s, const Launch &L, cudaStream_t st)
 {
     if (s == Step::REPLACE_CG || s == Step::REPLACE_BI) launch_replace(s == Step::REPLACE_BI, L, st);
@@ -441,12 +450,27 @@ int launch_slab_depth(const std::vector<VolSpec> &vols, const std::vector<JobSpe
     return zc;
 }
 
+// The one-sweep MIXED CG (OpCGF) is opt-in (FAST_TAU_CG_FUSED=1): its
+// sweep is 7 % faster than the two classic ones (415 against 447 us on the
+// 256^3 three-direction benchmark), but restarting at every residual
+// replacement costs it about 4 % more iterations and four more vectors per
+// right-hand side; the batched and served workloads ran slower with it
+// (58.0 against 60.7 and 20.2 against 21.1 solves/s).
+bool cg_fused_enabled()
+{
+    static const int on = env_int("FAST_TAU_CG_FUSED", 0);
+    return on != 0;
+}
+
 size_t job_bytes(int64_t nx, int64_t ny, int64_t nz, int prec, int solver, int zc)
 {
     const bool mixed = prec == FAST_PREC_MIXED;
     const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
-    // CG: x, r, p x2; BiCGSTAB: x, r x2, r0, p x2, v x2 (+ t for MIXED)
-    const size_t nvec = (solver == FAST_SOLVER_CG) ? 4 : (mixed ? 9 : 8);
+    // CG: x, r, p x2; BiCGSTAB: x, r x2, r0, p x2, v x2 (+ t for MIXED);
+    // the one-sweep MIXED CG uses the MIXED BiCGSTAB set (r, s = v, w = t/r0
+    // ping-pong, p and x in place)
+    const bool fused = mixed && solver == FAST_SOLVER_CG && cg_fused_enabled();
+    const size_t nvec = (solver == FAST_SOLVER_CG && !fused) ? 4 : (mixed ? 9 : 8);
     const size_t NP = (size_t)(row_pitch(nx) * ny * nz);
     const Geometry G = make_geometry(nx, ny, nz, zc > 0 ? zc : slab_depth(nx, ny, nz));
     return nvec * align_up(NP * vec_t, 256) + (mixed ? 2 * align_up(NP * 8, 256) : 0) +
@@ -491,7 +515,8 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     J.r[0] = A.take(vbytes);
     J.p[0] = A.take(vbytes);
     J.p[1] = A.take(vbytes);
-    if (solver == FAST_SOLVER_BICGSTAB) {
+    const bool fused = mixed && solver == FAST_SOLVER_CG && cg_fused_enabled();
+    if (solver == FAST_SOLVER_BICGSTAB || fused) {
         J.r[1] = A.take(vbytes);
         J.r0 = A.take(vbytes);
         J.v[0] = A.take(vbytes);
@@ -500,7 +525,7 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     if (mixed) {
         J.x64[0] = A.take(v64);
         J.x64[1] = A.take(v64);
-        if (solver == FAST_SOLVER_BICGSTAB) J.t = A.take(vbytes);
+        if (solver == FAST_SOLVER_BICGSTAB || fused) J.t = A.take(vbytes);
     }
     J.part = (double *)A.take((size_t)G.ntiles * NPART * sizeof(double));
     if (A.off > A.cap) return fail(FAST_CUDA_ERROR, "internal: device plan overflow");
@@ -510,7 +535,7 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R], J.r[0], es, nx, ny, nz, pitch);
     if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P], J.p[0], es, nx, ny, nz, pitch);
     if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P + 1], J.p[1], es, nx, ny, nz, pitch);
-    if (ts == FAST_OK && solver == FAST_SOLVER_BICGSTAB) {
+    if (ts == FAST_OK && (solver == FAST_SOLVER_BICGSTAB || fused)) {
         ts = tensor_map(&J.tm[TM_R + 1], J.r[1], es, nx, ny, nz, pitch);
         if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R0], J.r0, es, nx, ny, nz, pitch);
         if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_V], J.v[0], es, nx, ny, nz, pitch);
@@ -543,6 +568,7 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     const double cmin = env_double("FAST_TAU_SHADOW_COS", 1e-6);
     S.cos2_min = cmin * cmin;
     S.inner_mode = mixed ? 1 : 0;
+    S.cg_fused = fused ? 1 : 0;
     // MIXED BiCGSTAB: no update is pending before the first replacement.
     S.alpha = 0.0;
     S.omega = 0.0;
@@ -655,8 +681,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
         // the recursion asked for it.
         launch_counted(FAST_K_INIT64, st, [&] { launch_init64(L, st); });
         std::vector<Step> steps;
-        if (solver == FAST_SOLVER_CG) steps = {Step::REPLACE_CG, Step::CG1, Step::CG2};
-        else steps = {Step::REPLACE_BI, Step::BI_K1, Step::BI_K2};
+        steps = mixed_steps(solver);
         status = iterate(E, L, nj, d_sc, steps, dispatch_mixed, P.max_iter);
     }
     if (status == FAST_OK)

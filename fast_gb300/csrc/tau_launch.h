@@ -6,7 +6,7 @@
 
 namespace ft {
 
-enum class Step { INIT_CG, INIT_BI, CG1, CG2, BI_RESTART, BI1, BI2, BI3, REPLACE_CG, REPLACE_BI, BI_K1, BI_K2 };
+enum class Step { INIT_CG, INIT_BI, CG1, CG2, BI_RESTART, BI1, BI2, BI3, REPLACE_CG, REPLACE_BI, BI_K1, BI_K2, CG_F };
 
 // Pure-precision solves: `f64` selects double, otherwise float (scalars in
 // the solve precision, as the reference's T).

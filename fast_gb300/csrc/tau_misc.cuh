@@ -58,7 +58,9 @@ struct OpReplace {
         F = faces_of<T>(J);
         const Scalars &sc = *J.sc;
         const int cur = sc.x64_cur;
-        const int par = BICG ? (int)(sc.iter & 1) : 0;
+        // the residual goes where the next kernel reads it: r[iter & 1] for
+        // BiCGSTAB and the one-sweep CG, r[0] for the two-sweep CG
+        const int par = (BICG || sc.cg_fused) ? (int)(sc.iter & 1) : 0;
         tmap[0] = &J.tm[TM_X64 + cur];
         tmap[1] = &J.tm[TM_X];
         tmap[2] = &J.tm[TM_CODE];
@@ -130,6 +132,11 @@ struct OpReplace {
         if (sc.iter >= sc.max_iter) { sc.state = MAXITER; return; }
         sc.rsq = t[0];
         sc.rsq_max = t[0];
+        if (sc.cg_fused) {
+            // the one-sweep CG restarts from the replaced residual
+            sc.k1_mode = 1;
+            return;
+        }
         if (mode == 2) {
             // Fresh Krylov space from the true residual: p (and v) are zero,
             // so the next step-1 kernel forms p = r (CG: p = z).

@@ -1433,4 +1433,144 @@ struct OpBiK2 {
     __device__ static void finish(Scalars &sc, const double (&t)[NV]) { bicg2_k2_finish(sc, t[0], t[1], t[2], t[3]); }
 };
 
+// ===========================================================================
+// MIXED CG in one sweep per iteration: Chronopoulos & Gear's CG (one
+// reduction phase per iteration), with w = A u (u = r/diag) and s = A p kept
+// as vectors so that the sweep's only stencil is the one on u.  Sweep k
+// applies the pending updates of iteration k-1 pointwise,
+//   p = u + beta p,  s = w + beta s,  e += alpha p,  r -= alpha s
+// (u from the incoming r, w as stored), then forms u_k = r_k/diag (at the
+// halo too, from the same pointwise update of its r, s, w), w_k = A u_k and
+// the dots gamma = r_k.u_k, delta = w_k.u_k and |r_k|^2.  The finisher turns
+// them into beta = gamma/gamma_old and alpha = gamma/(delta - beta
+// gamma/alpha_old) for the next sweep.  After a residual replacement
+// (k1_mode = 1) the sweep restarts from the replaced residual: no pending
+// update, e = 0, and beta = 0 for the next sweep (p and s are written as 0).
+// Streams: r, s, w (ping-pong, read with a halo), p, e (in place), code.
+// ===========================================================================
+__device__ __forceinline__ void cgf_finish(Scalars &sc, double gamma, double delta, double rr)
+{
+    const bool restart = sc.k1_mode != 0;
+    sc.k1_mode = 0;
+    sc.e_reset = 0;
+    sc.rsq = rr;
+    sc.iter += 1;
+    if (!(rr <= sc.div_thresh)) {  // non-finite or exploding: restart from the true residual
+        sc.restarts += 1;
+        sc.replace = 2;
+        return;
+    }
+    double beta = 0.0, den = delta;
+    if (!restart) {
+        beta = gamma / sc.zr;
+        den = delta - beta * gamma / sc.alpha;
+    }
+    const double alpha = gamma / den;
+    if (!(fabs(alpha) < 1e300) || !(fabs(beta) < 1e300) || alpha == 0.0) {
+        sc.restarts += 1;
+        sc.replace = 2;
+        return;
+    }
+    sc.beta = beta;
+    sc.alpha = alpha;
+    sc.zr = gamma;
+    mixed_request(sc, rr, 2);
+}
+
+#ifndef FAST_TAU_HINT_CGF
+#define FAST_TAU_HINT_CGF 0
+#endif
+struct OpCGF {
+    using T = float;
+    static constexpr bool FB = true;
+    static constexpr uint32_t wait_hint_ns = FAST_TAU_HINT_CGF;
+    using SL = Streams<4, 4, 4, 4, 4, 1>;  // r, s, w, p, e, code
+    static constexpr int NV = 3;
+    using Shared = NoShared;
+    struct Vals { float r, s, w, p, e; uint32_t code; };
+    struct Own { uint32_t code; float rk, pk, sk, ek; };
+    struct Out { float r, p, s, w, e; };
+    const CUtensorMap *tmap[SL::N];
+    Faces<T> F;
+    float *rout, *sout, *wout, *pio, *eio;
+    float a, bt;
+    bool restart, ezero;
+    Acc<float> g_, d_, rr_;
+
+    __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
+    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<float, SL, 0>(st, p, a.r, b.r);
+        sv2<float, SL, 1>(st, p, a.s, b.s);
+        sv2<float, SL, 2>(st, p, a.w, b.w);
+        sv2<float, SL, 3>(st, p, a.p, b.p);
+        sv2<float, SL, 4>(st, p, a.e, b.e);
+        load_code2<SL, 5>(st, p, a.code, b.code);
+    }
+    __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a)
+    {
+        a.r = sv<float, SL, 0>(st, p);
+        a.s = sv<float, SL, 1>(st, p);
+        a.w = sv<float, SL, 2>(st, p);
+        a.code = sv<uint8_t, SL, 5>(st, p);
+    }
+    __device__ void init(const Job &J, Shared &)
+    {
+        F = faces_of<T>(J);
+        const Scalars &sc = *J.sc;
+        const int par = (int)(sc.iter & 1);
+        tmap[0] = &J.tm[TM_R + par];
+        tmap[1] = &J.tm[TM_V + par];
+        tmap[2] = &J.tm[par ? TM_R0 : TM_T];
+        tmap[3] = &J.tm[TM_P];
+        tmap[4] = &J.tm[TM_X];
+        tmap[5] = &J.tm[TM_CODE];
+        rout = (float *)J.r[par ^ 1];
+        sout = (float *)J.v[par ^ 1];
+        wout = (float *)(par ? J.t : J.r0);
+        pio = (float *)J.p[0];
+        eio = (float *)J.x;
+        restart = sc.k1_mode != 0;
+        ezero = sc.e_reset != 0;
+        a = restart ? 0.f : (float)sc.alpha;
+        bt = restart ? 0.f : (float)sc.beta;
+    }
+    __device__ float rk(const Vals &v) const { return restart ? v.r : v.r - a * (v.w + bt * v.s); }
+    __device__ T field(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps) const
+    {
+        return rk(v) * inv_of<T, FB>(C, g, v.code, ps);
+    }
+    __device__ Own own(const Geo &g, const Coef<T> &C, Shared &, const Vals &v, const Pos &ps, T &f) const
+    {
+        const float inv = inv_of<T, FB>(C, g, v.code, ps);
+        const float r = rk(v);
+        f = r * inv;
+        const float e0 = ezero ? 0.f : v.e;
+        if (restart) return Own{v.code, r, 0.f, 0.f, e0};
+        const float pk = v.r * inv + bt * v.p;  // p_{k-1} = u_{k-1} + beta p
+        return Own{v.code, r, pk, v.w + bt * v.s, e0 + a * pk};
+    }
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc, T fxp, T fxm,
+                         T fyp, T fym, T fzp, T fzm)
+    {
+        const T d = diag_of<T, FB>(C, g, o.code, ps);
+        const T w = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        g_.add_prod(o.rk, fc);
+        d_.add_prod(w, fc);
+        rr_.add_prod(o.rk, o.rk);
+        return Out{o.rk, o.pk, o.sk, w, o.ek};
+    }
+    __device__ void store(int64_t i, const Out &a_, const Out &b_, bool v0, bool v1)
+    {
+        store2<float>(rout, i, a_.r, b_.r, v0, v1);
+        store2<float>(sout, i, a_.s, b_.s, v0, v1);
+        store2<float>(wout, i, a_.w, b_.w, v0, v1);
+        store2<float>(pio, i, a_.p, b_.p, v0, v1);
+        store2<float>(eio, i, a_.e, b_.e, v0, v1);
+    }
+    __device__ void partials(T (&v_)[NV]) const { v_[0] = g_.hi(); v_[1] = d_.hi(); v_[2] = rr_.hi(); }
+    __device__ static void finish(Scalars &sc, const double (&t)[NV]) { cgf_finish(sc, t[0], t[1], t[2]); }
+};
+
 }  // namespace ft

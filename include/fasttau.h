@@ -215,7 +215,7 @@ FAST_API int fast_porosity(const uint8_t *mask, int64_t nx, int64_t ny, int64_t 
 enum {
     FAST_K_CODE = 0, FAST_K_INIT = 1, FAST_K_CG1 = 2, FAST_K_CG2 = 3, FAST_K_BI_RESTART = 4,
     FAST_K_BI1 = 5, FAST_K_BI2 = 6, FAST_K_BI3 = 7, FAST_K_REPLACE = 8, FAST_K_INIT64 = 9,
-    FAST_K_TAU = 10, FAST_K_COUNT = 16
+    FAST_K_TAU = 10, FAST_K_CGF = 11, FAST_K_COUNT = 16
 };
 
 /* Launch statistics of the calling thread's last solve. */

@@ -17,12 +17,15 @@ Tolerances:
     the 256^3 benchmark volume.
 """
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
 
 import fast_gb300 as ft
 from fast_gb300 import volumes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 pytestmark = pytest.mark.gpu
 
@@ -197,3 +200,27 @@ def test_non_convergence_and_errors(gpu):
     prm.solver = 7
     assert L.fast_tau_solve(m.ctypes.data_as(C.c_void_p), 4, 4, 4, C.byref(prm), None, None, None, None) == ft.Status.BAD_ARG
     assert b"solver" in L.fast_last_error()
+
+
+@pytest.mark.gpu
+def test_mixed_cg_one_sweep_option(gpu, oracle, tmp_path):
+    """The opt-in one-sweep MIXED CG (FAST_TAU_CG_FUSED=1, read once per
+    process, hence a child process) converges to the FP64 oracle's tau."""
+    import subprocess
+    import sys
+    m = np.empty((40, 44, 48), np.uint8)
+    assert gpu.fast_gen_spheres(m.ctypes.data_as(C.c_void_p), 48, 44, 40, 21, 3.0, 5.0, 0.5) == 0
+    np.save(tmp_path / "m.npy", m)
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, %r)\n"
+        "import fast_gb300 as ft\n"
+        "m = np.load(%r)\n"
+        "p = ft.TortuosityParams(dir=ft.Dir.X_POS, tolerance=1e-8, precision=ft.Precision.MIXED)\n"
+        "print(ft.get_tortuosity(m, p, ft.DSOLVER_CG))\n" % (ROOT, str(tmp_path / "m.npy")))
+    env = dict(os.environ, FAST_TAU_CG_FUSED="1")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stderr
+    tau = float(r.stdout.strip().splitlines()[-1])
+    ref = oracle.get_tortuosity(m, dir=0, tol=1e-10)
+    assert ref["status"] == 0
+    assert rel(tau, ref["tau"]) <= 1e-5
