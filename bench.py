@@ -387,7 +387,7 @@ C_RESULT_BYTES = 40  # sizeof(fast_tau_result)
 # --set full capture of a one-direction launch of the same volume
 # (profiles/), scaled by 3 to the three right-hand sides a bench launch
 # processes (traffic grows with the voxels).
-NCU_TRAFFIC = {"bi1": 3 * 670.4e6, "bi2": 3 * 274.4e6}
+NCU_TRAFFIC = {"bi1": 3 * 669.7e6, "bi2": 3 * 275.3e6}
 
 
 # ---------------------------------------------------------------------------
