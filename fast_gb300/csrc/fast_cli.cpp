@@ -12,8 +12,11 @@
 // face (rad; radTime = the labelling + tensor time / 6) and a DIR_NONE row
 // with the whole solid/pore area; with --basic, one row per direction
 // carrying the whole area (radBasic, radBasicTime) and no dir column.
-// Columns are sorted by name as the reference's row map sorts them.  --mesh
-// (OBJ export) and --segmentinfo are not provided.
+// Columns are sorted by name as the reference's row map sorts them.  With
+// --segmentinfo FILE the rows gain segmentVolumeRatio (volume fraction of the
+// pore components not touching that face) and FILE gets one row per component
+// not touching every face (getCCLSegmentInfo, VolumeSegmentation.cpp:135-215).
+// --mesh (OBJ export) is not provided.
 //
 // slice rows (SliceModule.h:34-240): every sub-volume of --size at origins
 // begin, begin + stride, ... with origin + size <= end (end defaults to the
@@ -287,10 +290,74 @@ std::string fmt(T v)
     return o.str();
 }
 
-// AlphaModule::getAlpha (AlphaModule.h:28-179) without the mesh and
-// segment-info exports.
+// One component of getCCLSegmentInfo (fastlib/src/volume/
+// VolumeSegmentation.cpp:135-180): bounding box (max exclusive), voxel count,
+// whether the box reaches a face.
+struct SegInfo {
+    int64_t minb[3], maxb[3];
+    int64_t voxels = 0;
+    bool at_boundary = false;
+};
+
+// getVolumeCCL(mask, 255) on the GPU, then getCCLSegmentInfo over the labels
+// on the host, as the reference computes it (on retrieved labels).
+bool segment_info(const Vol &vol, std::vector<SegInfo> &info, std::vector<uint8_t> &boundary, std::string &err)
+{
+    const size_t n = (size_t)(vol.nx * vol.ny * vol.nz);
+    std::vector<uint32_t> labels(n);
+    uint32_t k = 0;
+    if (fast_ccl_label(vol.data.data(), vol.nx, vol.ny, vol.nz, 255, labels.data(), &k, nullptr, 0) != FAST_OK) {
+        err = fast_last_error();
+        return false;
+    }
+    boundary.assign((size_t)7 * k, 0);
+    if (fast_ccl_label(vol.data.data(), vol.nx, vol.ny, vol.nz, 255, nullptr, &k, boundary.data(), boundary.size()) !=
+        FAST_OK) {
+        err = fast_last_error();
+        return false;
+    }
+    const int64_t dim[3] = {vol.nx, vol.ny, vol.nz};
+    info.assign(k, SegInfo{});
+    for (SegInfo &g : info)
+        for (int a = 0; a < 3; a++) {
+            g.minb[a] = dim[a];
+            g.maxb[a] = 0;
+        }
+    size_t i = 0;
+    for (int64_t z = 0; z < vol.nz; z++)
+        for (int64_t y = 0; y < vol.ny; y++)
+            for (int64_t x = 0; x < vol.nx; x++, i++) {
+                SegInfo &g = info[labels[i]];
+                g.voxels++;
+                const int64_t p[3] = {x, y, z};
+                for (int a = 0; a < 3; a++) {
+                    g.minb[a] = std::min(g.minb[a], p[a]);
+                    g.maxb[a] = std::max(g.maxb[a], p[a]);
+                }
+            }
+    for (SegInfo &g : info) {
+        for (int a = 0; a < 3; a++) g.maxb[a] += 1;  // non-inclusive bounds
+        g.at_boundary = g.maxb[0] == dim[0] || g.maxb[1] == dim[1] || g.maxb[2] == dim[2] || g.minb[0] == 0 ||
+                        g.minb[1] == 0 || g.minb[2] == 0;
+    }
+    return true;
+}
+
+// getCCLSegmentRatio of filterSegmentInfo(info, ccl, dir) (VolumeSegmentation.
+// cpp:182-215): the volume fraction of the components (label >= 1) that do
+// not touch face `row` (row 6: not every face).
+double segment_ratio(const std::vector<SegInfo> &info, const std::vector<uint8_t> &boundary, int row, int64_t n)
+{
+    const size_t k = info.size();
+    int64_t vox = 0;
+    for (size_t l = 1; l < k; l++)
+        if (!boundary[(size_t)row * k + l]) vox += info[l].voxels;
+    return (double)(float)((float)vox / (float)n);
+}
+
+// AlphaModule::getAlpha (AlphaModule.h:28-179) without the mesh export.
 int run_alpha(const std::string &name, const Vol &vol, const std::vector<int32_t> &dirs, bool basic,
-              const std::string &out_path)
+              const std::string &out_path, const std::string &info_path)
 {
     double phi = 0.0;
     if (fast_porosity(vol.data.data(), vol.nx, vol.ny, vol.nz, &phi, nullptr) != FAST_OK) {
@@ -316,11 +383,22 @@ int run_alpha(const std::string &name, const Vol &vol, const std::vector<int32_t
             std::cerr << "error: " << fast_last_error() << "\n";
             return 1;
         }
+        std::vector<SegInfo> info;
+        std::vector<uint8_t> boundary;
+        const int64_t n = vol.nx * vol.ny * vol.nz;
+        if (!info_path.empty()) {
+            std::string err;
+            if (!segment_info(vol, info, boundary, err)) {
+                std::cerr << "error: " << err << "\n";
+                return 1;
+            }
+        }
         for (int32_t d : dirs) {
             auto row = common;
             row.push_back({"rad", fmt(tensor[d])});
             row.push_back({"radTime", fmt(rad_time / 6.0f)});
             row.push_back({"dir", dir_string(d)});
+            if (!info.empty()) row.push_back({"segmentVolumeRatio", fmt((float)segment_ratio(info, boundary, d, n))});
             write_map_row(out_path, first_stdout, row);
         }
         double area = 0.0, secs = 0.0;
@@ -332,7 +410,20 @@ int run_alpha(const std::string &name, const Vol &vol, const std::vector<int32_t
         row.push_back({"rad", fmt((float)area)});
         row.push_back({"radTime", fmt(secs)});
         row.push_back({"dir", "DIR_NONE"});
+        if (!info.empty()) row.push_back({"segmentVolumeRatio", fmt((float)segment_ratio(info, boundary, 6, n))});
         write_map_row(out_path, first_stdout, row);
+        // The components that do not touch every face (filterSegmentInfo with
+        // DIR_NONE), one row each, to the segment-info CSV.
+        bool info_first = true;
+        const size_t k = info.size();
+        for (size_t l = 1; l < k; l++) {
+            if (boundary[6 * k + l]) continue;
+            const SegInfo &g = info[l];
+            write_map_row(info_path, info_first,
+                          {{"ID", name}, {"minX", fmt(g.minb[0])}, {"minY", fmt(g.minb[1])}, {"minZ", fmt(g.minb[2])},
+                           {"maxX", fmt(g.maxb[0])}, {"maxY", fmt(g.maxb[1])}, {"maxZ", fmt(g.maxb[2])},
+                           {"labelID", fmt(l)}, {"voxelNum", fmt(g.voxels)}, {"atBoundary", fmt((int)g.at_boundary)}});
+        }
     } else {
         double area = 0.0, secs = 0.0;
         if (timed_area(&area, &secs) != FAST_OK) {
@@ -496,6 +587,7 @@ int main(int argc, char **argv)
     int64_t slice_size[3] = {32, 32, 32}, slice_stride[3] = {1, 1, 1}, slice_begin[3] = {0, 0, 0},
             slice_end[3] = {0, 0, 0};
     std::string slice_out = "out";
+    std::string info_path;
 
     std::string input, dir = "x-", solver = "CG", precision = "double", out_path;
     int tol_exp = 6;
@@ -527,7 +619,8 @@ int main(int argc, char **argv)
         else if (a == "--begin" && action == "slice") parse3(next("--begin"), slice_begin);
         else if (a == "--end" && action == "slice") parse3(next("--end"), slice_end);
         else if (a == "--out" && action == "slice") slice_out = next("--out");
-        else if ((a == "--mesh" || a == "--segmentinfo") && action == "alpha") {
+        else if (a == "--segmentinfo" && action == "alpha") info_path = next("--segmentinfo");
+        else if (a == "--mesh" && action == "alpha") {
             std::cerr << "error: " << a << " is not provided\n";
             return 1;
         }
@@ -598,7 +691,7 @@ int main(int argc, char **argv)
         vol = crop(vol, lo, size);
     }
 
-    if (action == "alpha") return run_alpha(input, vol, get_dirs(dir), basic, out_path);
+    if (action == "alpha") return run_alpha(input, vol, get_dirs(dir), basic, out_path, info_path);
     if (action == "slice") return run_slice(input, vol, slice_size, slice_stride, slice_begin, slice_end, slice_out);
 
     fast_tau_params p;

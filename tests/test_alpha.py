@@ -177,3 +177,38 @@ def test_cli_alpha(gpu, oracle, tmp_path):
     rows = list(csv.DictReader(open(out2)))
     assert len(rows) == 2 and list(rows[0]) == ["ID", "dimx", "dimy", "dimz", "porosity", "radBasic", "radBasicTime"]
     assert float(rows[0]["radBasic"]) == pytest.approx(oracle.reactive_area(m), rel=1e-5)
+
+
+@pytest.mark.gpu
+def test_cli_alpha_segmentinfo(gpu, oracle, tmp_path):
+    from fast_gb300 import build
+    m = np.empty((22, 26, 30), np.uint8)
+    assert gpu.fast_gen_spheres(m.ctypes.data_as(C.c_void_p), 30, 26, 22, 8, 2.0, 4.0, 0.62) == Status.OK
+    p = str(tmp_path / "v.bin")
+    volume_io.save_volume_binary(p, m)
+    out, info = str(tmp_path / "a.csv"), str(tmp_path / "seg.csv")
+    r = subprocess.run([build.CLI, "alpha", p, "-d", "xy", "-o", out, "--segmentinfo", info], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    rows = list(csv.DictReader(open(out)))
+    assert list(rows[0])[-1] == "segmentVolumeRatio"
+    labels, k = oracle.ccl_label(m, 255)
+    table = oracle.ccl_boundary(labels, k)
+    counts = np.bincount(labels.ravel(), minlength=k)
+    n = m.size
+    for row, d in zip(rows, [X_POS, Y_POS, 6]):
+        want = counts[1:][table[d][1:] == 0].sum() / n
+        assert float(row["segmentVolumeRatio"]) == pytest.approx(want, rel=1e-5, abs=1e-7)
+    seg = list(csv.DictReader(open(info)))
+    assert list(seg[0]) == ["ID", "atBoundary", "labelID", "maxX", "maxY", "maxZ", "minX", "minY", "minZ",
+                            "voxelNum"]
+    want_ids = [l for l in range(1, k) if table[6][l] == 0]
+    assert [int(s["labelID"]) for s in seg] == want_ids
+    for s in seg[:20]:
+        l = int(s["labelID"])
+        z, y, x = np.nonzero(labels == l)
+        assert int(s["voxelNum"]) == len(x)
+        assert (int(s["minX"]), int(s["minY"]), int(s["minZ"])) == (x.min(), y.min(), z.min())
+        assert (int(s["maxX"]), int(s["maxY"]), int(s["maxZ"])) == (x.max() + 1, y.max() + 1, z.max() + 1)
+        at = x.min() == 0 or y.min() == 0 or z.min() == 0 or x.max() == 29 or y.max() == 25 or z.max() == 21
+        assert int(s["atBoundary"]) == int(at)
