@@ -109,6 +109,8 @@ SIGNATURES = {
                                             C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "fast_reactive_area_tensor_device": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_float,
                                                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]),
+    "fast_reactive_area_mesh": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_float, C.c_void_p,
+                                          C.c_uint64, C.POINTER(C.c_uint64)]),
     "fast_last_error": (C.c_char_p, []),
     "fast_version": (C.c_char_p, []),
     "fast_gen_spheres": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_double,

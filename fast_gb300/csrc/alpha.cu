@@ -47,6 +47,7 @@
 // two) and within 1/512 of 1/2 otherwise.  The engine uses exactly 1/2.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -618,9 +619,220 @@ int with_device_mask(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, F 
     return s;
 }
 
+// ---------------------------------------------------------------------------
+// Mesh export: the triangles themselves (getVolumeAreaMesh, fastlib/src/
+// volume/VolumeSurface.cpp:38-68, ___generateTriangles in fastlib/src/cuda/
+// VolumeSurface.cu:264-357).  Field = voxel != 0, corner values and cut
+// vertices as for the area; positions in the reference's mesh frame: a voxel
+// is dx = 1/max(n) wide on every axis and the grid is centred on the origin,
+// p = (dx i - dx n / 2, ...); one face normal per triangle,
+// normalize((v1 - v0) x (v2 - v0)).  Two passes with a fixed order: blocks
+// of 256 cells count their triangles, the host scans the block totals, and
+// each block writes its cells' triangles in cell order (12 floats each: three
+// vertices, then the normal).
+// ---------------------------------------------------------------------------
+constexpr int kMeshBlock = 256;
+
+struct MeshArgs {
+    const uint8_t *mask;
+    const McTable *table;
+    int nx, ny, nz, thr;
+    float iso, vx, vy, vz, dx;
+};
+
+__device__ __forceinline__ uint32_t mesh_counts(const MeshArgs &A, int64_t cell, int &cube, int &i, int &j, int &k)
+{
+    i = (int)(cell % A.nx);
+    j = (int)((cell / A.nx) % A.ny);
+    k = (int)(cell / ((int64_t)A.nx * A.ny));
+    uint32_t cnt = 0;
+    cube = 0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const int ox = (c & 1) ^ ((c >> 1) & 1), oy = (c >> 1) & 1, oz = c >> 2;
+        int n = 0;
+        for (int dz = -1; dz <= 0; dz++)
+            for (int dy = -1; dy <= 0; dy++)
+                for (int dxx = -1; dxx <= 0; dxx++) {
+                    int gx = i + ox + dxx, gy = j + oy + dy, gz = k + oz + dz;
+                    gx = gx < 0 ? 0 : (gx >= A.nx ? A.nx - 1 : gx);
+                    gy = gy < 0 ? 0 : (gy >= A.ny ? A.ny - 1 : gy);
+                    gz = gz < 0 ? 0 : (gz >= A.nz ? A.nz - 1 : gz);
+                    n += A.mask[((int64_t)gz * A.ny + gy) * A.nx + gx] != 0;
+                }
+        cnt |= (uint32_t)n << (4 * c);
+        cube |= (n < A.thr) << c;
+    }
+    return cnt;
+}
+
+__global__ void __launch_bounds__(kMeshBlock) mesh_count_kernel(MeshArgs A, int64_t ncell, uint32_t *block_tri)
+{
+    __shared__ uint32_t s[kMeshBlock];
+    const int64_t cell = (int64_t)blockIdx.x * kMeshBlock + threadIdx.x;
+    uint32_t nt = 0;
+    if (cell < ncell) {
+        int cube, i, j, k;
+        mesh_counts(A, cell, cube, i, j, k);
+        nt = A.table->ntri[cube];
+    }
+    s[threadIdx.x] = nt;
+    __syncthreads();
+    for (int w = kMeshBlock / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) block_tri[blockIdx.x] = s[0];
+}
+
+__global__ void __launch_bounds__(kMeshBlock) mesh_emit_kernel(MeshArgs A, int64_t ncell, const uint64_t *block_off,
+                                                               float *out)
+{
+    __shared__ uint32_t s[kMeshBlock];
+    const int64_t cell = (int64_t)blockIdx.x * kMeshBlock + threadIdx.x;
+    int cube = 0, i = 0, j = 0, k = 0;
+    uint32_t cnt = 0, nt = 0;
+    if (cell < ncell) {
+        cnt = mesh_counts(A, cell, cube, i, j, k);
+        nt = A.table->ntri[cube];
+    }
+    // exclusive scan of the counts in cell order (Hillis-Steele over the block)
+    s[threadIdx.x] = nt;
+    __syncthreads();
+    for (int o = 1; o < kMeshBlock; o <<= 1) {
+        const uint32_t v = threadIdx.x >= o ? s[threadIdx.x - o] : 0u;
+        __syncthreads();
+        s[threadIdx.x] += v;
+        __syncthreads();
+    }
+    const uint64_t base = block_off[blockIdx.x] + s[threadIdx.x] - nt;
+    if (nt == 0) return;
+    // positions in the mesh frame (VolumeSurface.cu:291-297)
+    const float px = __fsub_rn(__fmul_rn(A.dx, (float)i), __fmul_rn(0.5f, __fmul_rn(A.dx, (float)A.nx)));
+    const float py = __fsub_rn(__fmul_rn(A.dx, (float)j), __fmul_rn(0.5f, __fmul_rn(A.dx, (float)A.ny)));
+    const float pz = __fsub_rn(__fmul_rn(A.dx, (float)k), __fmul_rn(0.5f, __fmul_rn(A.dx, (float)A.nz)));
+    const float qx = __fadd_rn(px, A.dx), qy = __fadd_rn(py, A.dx), qz = __fadd_rn(pz, A.dx);
+    for (uint32_t t = 0; t < nt; t++) {
+        float v[3][3];
+        for (int q = 0; q < 3; q++) {
+            const int e = A.table->edge[cube][3 * t + q];
+            const int ca = edge_a(e), cb = edge_b(e);
+            const float fa = __fmul_rn((float)((cnt >> (4 * ca)) & 15u), 0.125f);
+            const float fb = __fmul_rn((float)((cnt >> (4 * cb)) & 15u), 0.125f);
+            const float x0 = ((ca & 1) ^ ((ca >> 1) & 1)) ? qx : px, y0 = ((ca >> 1) & 1) ? qy : py, z0 = (ca >> 2) ? qz : pz;
+            const float x1 = ((cb & 1) ^ ((cb >> 1) & 1)) ? qx : px, y1 = ((cb >> 1) & 1) ? qy : py, z1 = (cb >> 2) ? qz : pz;
+            if (fa == fb) {
+                v[q][0] = x0; v[q][1] = y0; v[q][2] = z0;
+            } else {
+                const float tt = __fdiv_rn(__fsub_rn(A.iso, fa), __fsub_rn(fb, fa));
+                v[q][0] = lerp1(x0, x1, tt);
+                v[q][1] = lerp1(y0, y1, tt);
+                v[q][2] = lerp1(z0, z1, tt);
+            }
+        }
+        const float ax = __fsub_rn(v[1][0], v[0][0]), ay = __fsub_rn(v[1][1], v[0][1]), az = __fsub_rn(v[1][2], v[0][2]);
+        const float bx = __fsub_rn(v[2][0], v[0][0]), by = __fsub_rn(v[2][1], v[0][1]), bz = __fsub_rn(v[2][2], v[0][2]);
+        const float cx = __fsub_rn(__fmul_rn(ay, bz), __fmul_rn(az, by));
+        const float cy = __fsub_rn(__fmul_rn(az, bx), __fmul_rn(ax, bz));
+        const float cz = __fsub_rn(__fmul_rn(ax, by), __fmul_rn(ay, bx));
+        const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)), __fmul_rn(cz, cz)));
+        const float inv = len > 0.f ? __fdiv_rn(1.0f, len) : 0.f;
+        float *o = out + (base + t) * 12;
+        for (int q = 0; q < 3; q++)
+            for (int a = 0; a < 3; a++) o[3 * q + a] = v[q][a];
+        o[9] = __fmul_rn(cx, inv);
+        o[10] = __fmul_rn(cy, inv);
+        o[11] = __fmul_rn(cz, inv);
+    }
+}
+
+int mesh_device(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, float iso, float *out, uint64_t capacity,
+                uint64_t *ntri, cudaStream_t st)
+{
+    std::call_once(g_table_once, [] { g_table = build_table(); });
+    const int64_t ncell = nx * ny * nz;
+    const int64_t nblocks = (ncell + kMeshBlock - 1) / kMeshBlock;
+    if (nblocks > INT32_MAX) return ft_fail(FAST_BAD_ARG, "volume too large for the mesh export");
+    MeshArgs A;
+    A.mask = d_mask;
+    A.nx = (int)nx;
+    A.ny = (int)ny;
+    A.nz = (int)nz;
+    A.iso = iso;
+    A.thr = 9;
+    for (int c = 8; c >= 0; c--)
+        if ((float)c * 0.125f >= iso) A.thr = c;
+    const int64_t maxdim = std::max(nx, std::max(ny, nz));
+    A.dx = 1.0f / (float)maxdim;
+    char *scratch = nullptr;
+    const size_t need = sizeof(McTable) + 256 + (size_t)nblocks * 4 + 256 + (size_t)nblocks * 8;
+    cudaError_t e = cudaMallocAsync((void **)&scratch, need, st);
+    if (e != cudaSuccess) return ft_fail(FAST_NOMEM, "mesh scratch: %s", cudaGetErrorString(e));
+    McTable *d_tab = (McTable *)scratch;
+    uint32_t *d_cnt = (uint32_t *)(scratch + sizeof(McTable) + 256);
+    uint64_t *d_off = (uint64_t *)((char *)d_cnt + ((size_t)nblocks * 4 + 255) / 256 * 256);
+    A.table = d_tab;
+    std::vector<uint32_t> cnt((size_t)nblocks);
+    std::vector<uint64_t> off((size_t)nblocks);
+    int s = FAST_OK;
+    e = cudaMemcpyAsync(d_tab, &g_table, sizeof(McTable), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        mesh_count_kernel<<<(unsigned)nblocks, kMeshBlock, 0, st>>>(A, ncell, d_cnt);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cnt.data(), d_cnt, (size_t)nblocks * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    uint64_t total = 0;
+    if (e == cudaSuccess) {
+        for (int64_t b = 0; b < nblocks; b++) {
+            off[(size_t)b] = total;
+            total += cnt[(size_t)b];
+        }
+        *ntri = total;
+        if (out && total > capacity)
+            s = ft_fail(FAST_BAD_ARG, "mesh buffer holds %llu triangles, %llu needed", (unsigned long long)capacity,
+                        (unsigned long long)total);
+        if (out && s == FAST_OK && total > 0) {
+            float *d_out = nullptr;
+            e = cudaMallocAsync((void **)&d_out, (size_t)total * 12 * sizeof(float), st);
+            if (e != cudaSuccess) {
+                s = ft_fail(FAST_NOMEM, "mesh triangles: %s", cudaGetErrorString(e));
+            } else {
+                e = cudaMemcpyAsync(d_off, off.data(), (size_t)nblocks * 8, cudaMemcpyHostToDevice, st);
+                if (e == cudaSuccess) {
+                    mesh_emit_kernel<<<(unsigned)nblocks, kMeshBlock, 0, st>>>(A, ncell, d_off, d_out);
+                    e = cudaGetLastError();
+                }
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(out, d_out, (size_t)total * 12 * sizeof(float), cudaMemcpyDeviceToHost, st);
+                cudaFreeAsync(d_out, st);
+            }
+        }
+    }
+    cudaFreeAsync(scratch, st);
+    const cudaError_t e2 = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = e2;
+    if (s == FAST_OK && e != cudaSuccess) s = ft_fail(FAST_CUDA_ERROR, "mesh: %s", cudaGetErrorString(e));
+    return s;
+}
+
 }  // namespace
 
 extern "C" {
+
+FAST_API int fast_reactive_area_mesh(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, float isovalue,
+                                     float *triangles, uint64_t capacity, uint64_t *ntri)
+{
+    ft_clear_error();
+    if (!mask) return ft_fail(FAST_NO_HOST_DATA, "mask is NULL");
+    if (!ntri) return ft_fail(FAST_BAD_ARG, "ntri is NULL");
+    int s = check_args(nx, ny, nz, isovalue);
+    if (s != FAST_OK) return s;
+    return with_device_mask(mask, nx, ny, nz, [&](const uint8_t *d, cudaStream_t st) {
+        return mesh_device(d, nx, ny, nz, isovalue, triangles, capacity, ntri, st);
+    });
+}
+
 
 FAST_API int fast_reactive_area_device(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, float isovalue,
                                        double *area, void *stream)

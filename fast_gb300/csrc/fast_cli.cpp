@@ -16,7 +16,8 @@
 // --segmentinfo FILE the rows gain segmentVolumeRatio (volume fraction of the
 // pore components not touching that face) and FILE gets one row per component
 // not touching every face (getCCLSegmentInfo, VolumeSegmentation.cpp:135-215).
-// --mesh (OBJ export) is not provided.
+// --mesh FILE writes the surface of the volume zero-padded by one voxel as a
+// Wavefront OBJ file (AlphaModule.h:150-173).
 //
 // slice rows (SliceModule.h:34-240): every sub-volume of --size at origins
 // begin, begin + stride, ... with origin + size <= end (end defaults to the
@@ -64,6 +65,7 @@
 #include <random>
 #include <sstream>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "fasttau.h"
@@ -355,9 +357,88 @@ double segment_ratio(const std::vector<SegInfo> &info, const std::vector<uint8_t
     return (double)(float)((float)vox / (float)n);
 }
 
-// AlphaModule::getAlpha (AlphaModule.h:28-179) without the mesh export.
+// The --mesh export (AlphaModule.h:150-173): the volume zero-padded by one
+// voxel (Volume::withZeroPadding), its surface triangles
+// (fast_reactive_area_mesh), written as CUDA_VBO::saveObj does
+// (fastlib/src/utility/DataPtr.cpp:684-740): vertices merged by exact
+// position, their face normals summed and normalised, "v", "vn" and "f"
+// lines.
+int export_mesh(const Vol &vol, const std::string &path)
+{
+    Vol pad;
+    pad.nx = vol.nx + 2;
+    pad.ny = vol.ny + 2;
+    pad.nz = vol.nz + 2;
+    pad.data.assign((size_t)(pad.nx * pad.ny * pad.nz), 0);
+    for (int64_t z = 0; z < vol.nz; z++)
+        for (int64_t y = 0; y < vol.ny; y++)
+            memcpy(&pad.data[(size_t)(1 + pad.nx * (y + 1 + pad.ny * (z + 1)))],
+                   &vol.data[(size_t)(vol.nx * (y + vol.ny * z))], (size_t)vol.nx);
+    uint64_t ntri = 0;
+    if (fast_reactive_area_mesh(pad.data.data(), pad.nx, pad.ny, pad.nz, 0.5f, nullptr, 0, &ntri) != FAST_OK) {
+        std::cerr << "error: " << fast_last_error() << "\n";
+        return 1;
+    }
+    if (ntri == 0) {
+        std::cerr << "Has no triangles" << std::endl;
+        return 0;
+    }
+    std::vector<float> tri((size_t)ntri * 12);
+    if (fast_reactive_area_mesh(pad.data.data(), pad.nx, pad.ny, pad.nz, 0.5f, tri.data(), ntri, &ntri) != FAST_OK) {
+        std::cerr << "error: " << fast_last_error() << "\n";
+        return 1;
+    }
+    std::cout << "Saving " << path << ", Vertices:" << ntri * 3 << std::endl;
+    struct Key {
+        uint32_t a, b, c;
+        bool operator==(const Key &o) const { return a == o.a && b == o.b && c == o.c; }
+    };
+    struct KeyHash {
+        size_t operator()(const Key &k) const { return ((size_t)k.a * 73856093u) ^ ((size_t)k.b * 19349663u) ^ ((size_t)k.c * 83492791u); }
+    };
+    std::unordered_map<Key, uint32_t, KeyHash> index;
+    std::vector<std::array<float, 3>> verts, normals;
+    std::vector<std::array<uint32_t, 3>> faces((size_t)ntri);
+    for (uint64_t t = 0; t < ntri; t++) {
+        const float *T = &tri[(size_t)t * 12];
+        for (int q = 0; q < 3; q++) {
+            Key k;
+            memcpy(&k.a, &T[3 * q], 4);
+            memcpy(&k.b, &T[3 * q + 1], 4);
+            memcpy(&k.c, &T[3 * q + 2], 4);
+            auto it = index.find(k);
+            uint32_t id;
+            if (it == index.end()) {
+                id = (uint32_t)verts.size();
+                verts.push_back({T[3 * q], T[3 * q + 1], T[3 * q + 2]});
+                normals.push_back({T[9], T[10], T[11]});
+                index.emplace(k, id);
+            } else {
+                id = it->second;
+                for (int a = 0; a < 3; a++) normals[id][a] += T[9 + a];
+            }
+            faces[(size_t)t][q] = id;
+        }
+    }
+    std::ofstream f(path);
+    if (!f.good()) {
+        std::cerr << "error: cannot write " << path << "\n";
+        return 1;
+    }
+    for (const auto &v : verts) f << "v " << v[0] << " " << v[1] << " " << v[2] << "\n";
+    for (auto n : normals) {
+        const float l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        const float inv = l > 0.f ? 1.0f / l : 0.f;
+        f << "vn " << n[0] * inv << " " << n[1] * inv << " " << n[2] * inv << "\n";
+    }
+    for (const auto &fc : faces) f << "f " << fc[0] + 1 << " " << fc[1] + 1 << " " << fc[2] + 1 << "\n";
+    std::cout << "Done." << std::endl;
+    return 0;
+}
+
+// AlphaModule::getAlpha (AlphaModule.h:28-179).
 int run_alpha(const std::string &name, const Vol &vol, const std::vector<int32_t> &dirs, bool basic,
-              const std::string &out_path, const std::string &info_path)
+              const std::string &out_path, const std::string &info_path, const std::string &mesh_path)
 {
     double phi = 0.0;
     if (fast_porosity(vol.data.data(), vol.nx, vol.ny, vol.nz, &phi, nullptr) != FAST_OK) {
@@ -437,6 +518,7 @@ int run_alpha(const std::string &name, const Vol &vol, const std::vector<int32_t
             write_map_row(out_path, first_stdout, row);
         }
     }
+    if (!mesh_path.empty()) return export_mesh(vol, mesh_path);
     return 0;
 }
 
@@ -587,7 +669,7 @@ int main(int argc, char **argv)
     int64_t slice_size[3] = {32, 32, 32}, slice_stride[3] = {1, 1, 1}, slice_begin[3] = {0, 0, 0},
             slice_end[3] = {0, 0, 0};
     std::string slice_out = "out";
-    std::string info_path;
+    std::string info_path, mesh_path;
 
     std::string input, dir = "x-", solver = "CG", precision = "double", out_path;
     int tol_exp = 6;
@@ -620,10 +702,7 @@ int main(int argc, char **argv)
         else if (a == "--end" && action == "slice") parse3(next("--end"), slice_end);
         else if (a == "--out" && action == "slice") slice_out = next("--out");
         else if (a == "--segmentinfo" && action == "alpha") info_path = next("--segmentinfo");
-        else if (a == "--mesh" && action == "alpha") {
-            std::cerr << "error: " << a << " is not provided\n";
-            return 1;
-        }
+        else if (a == "--mesh" && action == "alpha") mesh_path = next("--mesh");
         else if (a == "-j" || a == "--cputhreads") next("-j");
         else if (a == "--sub") has_sub = parse3(next("--sub"), sub);
         else if (a == "--origin") has_origin = parse3(next("--origin"), origin);
@@ -691,7 +770,7 @@ int main(int argc, char **argv)
         vol = crop(vol, lo, size);
     }
 
-    if (action == "alpha") return run_alpha(input, vol, get_dirs(dir), basic, out_path, info_path);
+    if (action == "alpha") return run_alpha(input, vol, get_dirs(dir), basic, out_path, info_path, mesh_path);
     if (action == "slice") return run_slice(input, vol, slice_size, slice_stride, slice_begin, slice_end, slice_out);
 
     fast_tau_params p;

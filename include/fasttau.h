@@ -337,6 +337,16 @@ FAST_API int fast_reactive_area_device(const uint8_t *d_mask, int64_t nx, int64_
 FAST_API int fast_reactive_area_tensor(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, float isovalue,
                                        double *tensor, double *area_solid);
 
+/* getVolumeAreaMesh(mask, false, mask.dim(), isovalue) (fastlib/src/volume/
+ * VolumeSurface.cpp:38-68): the triangles of the same surface, 12 floats each
+ * (vertices v0, v1, v2, then the unit face normal), in the reference's mesh
+ * frame (voxel size 1/max(nx, ny, nz) on every axis, grid centred on the
+ * origin), in cell order.  *ntri gets the count; triangles (host, capacity
+ * triangles) may be NULL to ask for the count only.  `fast alpha --mesh`
+ * writes them (of the volume zero-padded by one voxel) as an OBJ file. */
+FAST_API int fast_reactive_area_mesh(const uint8_t *mask, int64_t nx, int64_t ny, int64_t nz, float isovalue,
+                                     float *triangles, uint64_t capacity, uint64_t *ntri);
+
 /* The same on a DEVICE mask (stream as above; synchronised). */
 FAST_API int fast_reactive_area_tensor_device(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz,
                                               float isovalue, double *tensor, double *area_solid, void *stream);

@@ -212,3 +212,65 @@ def test_cli_alpha_segmentinfo(gpu, oracle, tmp_path):
         assert (int(s["maxX"]), int(s["maxY"]), int(s["maxZ"])) == (x.max() + 1, y.max() + 1, z.max() + 1)
         at = x.min() == 0 or y.min() == 0 or z.min() == 0 or x.max() == 29 or y.max() == 25 or z.max() == 21
         assert int(s["atBoundary"]) == int(at)
+
+
+@pytest.mark.gpu
+def test_cli_alpha_mesh(gpu, oracle, tmp_path):
+    from collections import Counter
+    from fast_gb300 import build
+    m = np.empty((14, 16, 18), np.uint8)
+    assert gpu.fast_gen_spheres(m.ctypes.data_as(C.c_void_p), 18, 16, 14, 4, 2.0, 3.5, 0.45) == Status.OK
+    p = str(tmp_path / "v.bin")
+    volume_io.save_volume_binary(p, m)
+    obj = str(tmp_path / "s.obj")
+    r = subprocess.run([build.CLI, "alpha", p, "--basic", "-o", str(tmp_path / "a.csv"), "--mesh", obj],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert "Saving" in r.stdout and "Done." in r.stdout
+    v, vn, f = [], [], []
+    for line in open(obj):
+        tag, *vals = line.split()
+        if tag == "v":
+            v.append([float(x) for x in vals])
+        elif tag == "vn":
+            vn.append([float(x) for x in vals])
+        elif tag == "f":
+            f.append([int(x) - 1 for x in vals])
+    v, vn, f = np.array(v), np.array(vn), np.array(f)
+    assert len(v) == len(vn) and len(f) > 0 and f.min() >= 0 and f.max() < len(v)
+    # unit normals, or zero where a vertex only belongs to zero-area
+    # triangles (cut points that coincide when a corner equals the isovalue)
+    nrm = np.linalg.norm(vn, axis=1)
+    assert np.all((np.abs(nrm - 1.0) < 1e-4) | (nrm == 0.0))
+    # mesh frame: voxel size 1/max(padded dims) on every axis, centred
+    pad = np.zeros((16, 18, 20), np.uint8)
+    pad[1:-1, 1:-1, 1:-1] = m
+    assert np.abs(v).max() <= 0.5 + 1e-6
+    # the area of the OBJ triangles is the oracle's area of the padded field,
+    # rescaled from per-axis units (1/n_a) to the mesh frame (1/max n)
+    a = v[f[:, 1]] - v[f[:, 0]]
+    b = v[f[:, 2]] - v[f[:, 0]]
+    area_obj = 0.5 * np.linalg.norm(np.cross(a, b), axis=1).sum()
+    nz, ny, nx = pad.shape
+    d = 1.0 / max(pad.shape)
+    scale = np.array([nx * d, ny * d, nz * d])          # mesh frame = per-axis frame * scale
+    # per-triangle rescaling is anisotropic: compare through the oracle's own
+    # triangle areas only when the volume is cubic; here check against a
+    # direct recomputation in the per-axis frame instead
+    area_axis = 0.5 * np.linalg.norm(np.cross(a / scale, b / scale), axis=1).sum()
+    assert area_axis == pytest.approx(oracle.reactive_area(pad), rel=2e-4)
+    assert area_obj > 0
+    # closed surface: the boundary of the triangle set is empty, i.e. every
+    # edge (by rounded position) of a nonzero-area triangle occurs an even
+    # number of times (two, or more where surface sheets touch along an edge)
+    key = np.round(v / d * 4096).astype(np.int64)
+    nonzero = np.linalg.norm(np.cross(a, b), axis=1) > 1e-12
+    edges = Counter()
+    for t in f[nonzero]:
+        pts = [tuple(key[i]) for i in t]
+        for e in range(3):
+            u, w = pts[e], pts[(e + 1) % 3]
+            if u != w:
+                edges[(min(u, w), max(u, w))] += 1
+    assert edges and all(c % 2 == 0 for c in edges.values())
+    assert sum(c == 2 for c in edges.values()) > 0.95 * len(edges)
