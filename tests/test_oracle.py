@@ -186,3 +186,87 @@ def test_ccl_boundary_table(oracle):
     assert b[1, corner] and b[3, corner] and b[5, corner] and not b[0, corner]
     assert b[0, bar] and b[1, bar] and not b[2, bar]
     assert not b[6].any()  # no label touches all six faces
+
+
+def _scipy_tau(m, d, d0=1.0, d1=D1):
+    """The reference discretisation assembled here from its rules, not from
+    the oracle (Diffusion.cpp:94-139, Diffusion.cuh:85-122,
+    VolumeMeasures.cpp:160-275), in h = 1 units: interior face coefficient
+    (D_n + D_i)/2; a domain face on the primary axis is a half cell (2 D_i) on
+    the diagonal, with b = -2 D_i on the inflow plane; other domain faces are
+    zero-flux.  Direct solve, then the tau flux average."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    nz, ny, nx = m.shape
+    dims = (nx, ny, nz)
+    k, sgn = d // 2, (1 if d % 2 == 0 else -1)
+    D = np.where(m.reshape(-1) != 0, d1, d0)
+    N = m.size
+    stride = (1, nx, nx * ny)
+    idx = np.arange(N)
+    coord = (idx % nx, (idx // nx) % ny, idx // (nx * ny))
+    rows, cols, vals = [], [], []
+    diag = np.zeros(N)
+    b = np.zeros(N)
+    for a in range(3):
+        for s in (1, -1):
+            c = coord[a]
+            inside = (c + s >= 0) & (c + s < dims[a])
+            nb = idx + s * stride[a]
+            cf = np.where(inside, 0.5 * (D[np.where(inside, nb, idx)] + D), 0.0)
+            rows.append(idx[inside]); cols.append(nb[inside]); vals.append(cf[inside])
+            diag -= cf
+            if a == k:
+                edge = ~inside
+                diag[edge] -= 2 * D[edge]
+    # inflow plane: c = 1 at the begin face (k = 0 for +, k = n-1 for -); the
+    # reference's `else if` gives a one-plane axis only the begin term
+    ck = coord[k]
+    if sgn > 0:
+        b[ck == 0] = -2 * D[ck == 0]
+    else:
+        first = ck == dims[k] - 1
+        if dims[k] == 1:
+            first = np.zeros(N, bool)   # cBegin = 0 and the else-branch is not taken
+        b[first] = -2 * D[first]
+    if not b.any():
+        return None  # zero right-hand side: the reference's solver reports failure (tau = 0)
+    A = sp.csr_matrix((np.concatenate(vals + [diag]),
+                       (np.concatenate(rows + [idx]), np.concatenate(cols + [idx]))), shape=(N, N))
+    x = spl.spsolve(A.tocsc(), b)
+    # tau (VolumeMeasures.cpp:185-271): flux D_cell (c - c_next)/dx per voxel,
+    # c_next one step along the direction, 0 with dx = 1/2 past the last plane
+    nxt = idx + sgn * stride[k]
+    last = (ck + sgn < 0) | (ck + sgn >= dims[k])
+    cn = np.where(last, 0.0, x[np.where(last, idx, nxt)])
+    dx = np.where(last, 0.5, 1.0)
+    dcell = np.where(m.reshape(-1) != 0, d1, d0)
+    f = dcell * (x - cn) / dx
+    n_plane = N // dims[k]
+    dc = sum(f[ck == p].sum() / n_plane for p in range(dims[k])) / dims[k]
+    phi = (m == 0).mean()
+    return phi / (dc * dims[k])
+
+
+def test_independent_scipy_assembly(oracle):
+    """Known-answer pin of the oracle against a second, independent assembly
+    of the reference discretisation (random small volumes, every direction)."""
+    hyp = pytest.importorskip("hypothesis")
+    from hypothesis import given, settings, strategies as st
+
+    @settings(max_examples=40, deadline=None, derandomize=True)
+    @given(st.integers(1, 6), st.integers(1, 6), st.integers(1, 6), st.integers(0, 5), st.integers(0, 2**31 - 1),
+           st.floats(0.0, 0.8))
+    def check(nx, ny, nz, d, seed, frac):
+        m = ((np.random.default_rng(seed).random((nz, ny, nx)) < frac) * 255).astype(np.uint8)
+        if not (m == 0).any():
+            return
+        ref = _scipy_tau(m, d)
+        got = oracle.get_tortuosity(m, dir=d, solver=oracle.CG, tol=1e-14, max_iter=100000)
+        if ref is None:
+            assert got["status"] != 0 and got["tau"] == 0.0
+            return
+        assert got["status"] == 0
+        assert rel(got["tau"], ref) < 1e-8, (m.shape, d, got["tau"], ref)
+
+    check()
