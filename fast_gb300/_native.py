@@ -121,7 +121,9 @@ SIGNATURES = {
 
 
 def lib_path() -> str:
-    return _build.LIB
+    """The in-tree build, or FAST_TAU_LIB (another build of the same library,
+    e.g. one compiled with FAST_TAU_BOUNDS_CHECK)."""
+    return os.environ.get("FAST_TAU_LIB") or _build.LIB
 
 
 def lib():

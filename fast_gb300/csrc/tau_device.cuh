@@ -33,6 +33,29 @@ namespace ft {
 // ---------------------------------------------------------------------------
 constexpr int NBC = 7;  // boundary counts -2..4
 
+// FAST_TAU_BOUNDS_CHECK=1 builds check every global access that TMA does not
+// bound (the plain loads and stores): an index outside its array records the
+// site in the right-hand side's scalars (the first one to fail) and the access
+// is skipped; the host reports the record as FAST_CUDA_ERROR.  Off (and free)
+// by default.
+#ifndef FAST_TAU_BOUNDS_CHECK
+#define FAST_TAU_BOUNDS_CHECK 0
+#endif
+enum OobSite { OOB_SWEEP_STORE = 1, OOB_PARTIALS = 2, OOB_CODE = 3, OOB_INIT = 4, OOB_TAU = 5 };
+
+// [lo, hi] inside [0, n)?
+__device__ __forceinline__ bool ft_in(const Job &J, int64_t lo, int64_t hi, int64_t n, int site)
+{
+#if FAST_TAU_BOUNDS_CHECK
+    if (lo >= 0 && hi < n) return true;
+    atomicCAS(&J.sc->oob, 0, site);
+    return false;
+#else
+    (void)J; (void)lo; (void)hi; (void)n; (void)site;
+    return true;
+#endif
+}
+
 // Float-float number: value = hi + lo, |lo| <= ulp(hi) / 2, about 48
 // significant bits.  The MIXED residual replacement keeps its iterate and
 // evaluates b - A x in this form with FP32 instructions (error-free

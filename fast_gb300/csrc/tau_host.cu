@@ -743,6 +743,13 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
             const double dc = (S.flux_sum / (double)nplane) / (double)dimk;
             R.tau = (R.status == FAST_OK) ? phi / (dc * (double)dimk) : 0.0;
         }
+        if (S.oob) {  // bounds-check builds only
+            R.status = FAST_CUDA_ERROR;
+            R.tau = 0.0;
+            if (first_bad == FAST_OK)
+                first_bad = fail(FAST_CUDA_ERROR, "bounds check: right-hand side %d, access site %d out of range", j,
+                                 S.oob);
+        }
         if (R.status != FAST_OK && first_bad == FAST_OK) {
             first_bad = R.status;
             fail(R.status, "right-hand side %d (direction %d): solver %s after %llu iterations (|r|/|b| = %.3e)", j,

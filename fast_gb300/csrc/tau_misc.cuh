@@ -350,6 +350,7 @@ __global__ void __launch_bounds__(NTHREADS) code_kernel(Launch L)
         for (int z = t.z0; z < t.z1; ++z) {
             const int64_t i = (int64_t)x + sy * y + sz * z;
             const int64_t ic = (int64_t)x + (int64_t)J.pitch * ((int64_t)y + (int64_t)ny * z);
+            if (!ft_in(J, i, i, sz * nz, OOB_CODE) || !ft_in(J, ic, ic, (int64_t)J.pitch * ny * nz, OOB_CODE)) continue;
             const uint32_t self = __ldg(m + i) != 0;
             pores += self ? 0u : 1u;
             uint32_t c = self << SELF_BIT;
@@ -397,6 +398,7 @@ __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
         if (!t.v[k]) continue;
         for (int z = t.z0; z < t.z1; ++z) {
             const int64_t i = g.idx(t.gx + k, t.gy, z);
+            if (!ft_in(J, i, i, (int64_t)J.pitch * J.ny * J.nz, OOB_INIT)) continue;
             x64[i] = FF(x0_at<float>(g, t.gx + k, t.gy, z), 0.f);
             e[i] = 0.f;
             if (zt) {
@@ -456,9 +458,11 @@ __global__ void __launch_bounds__(NTHREADS) tau_kernel(Launch L, int use_x64)
         for (int z = t.z0; z < t.z1; ++z) {
             const int64_t i = g.idx(x, t.gy, z);
             const int kn = g.coord(x, t.gy, z) + g.sgn;
+            const int64_t np = (int64_t)g.P * g.ny * g.nz;
+            if (!ft_in(J, i, i, np, OOB_TAU)) continue;
             const double here = conc_at(c, i);
             double prev = 0.0, rdx = 2.0;  // 1/dx: dx = 0.5 past the last plane
-            if (kn >= 0 && kn < ext) {
+            if (kn >= 0 && kn < ext && ft_in(J, i + sstep, i + sstep, np, OOB_TAU)) {
                 prev = conc_at(c, i + sstep);
                 rdx = 1.0;
             }

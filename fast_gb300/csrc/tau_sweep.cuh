@@ -418,7 +418,7 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
             typename Op::Out r0{}, r1{};
             if (v0) r0 = op.apply(g, C, S, oc0, Pos{gx, gy, zs, bc0 + bczs}, fc0, fc1, left.b, up.a, dn.a, fp0, fm0);
             if (v1) r1 = op.apply(g, C, S, oc1, Pos{gx + 1, gy, zs, bc1 + bczs}, fc1, right.a, fc0, up.b, dn.b, fp1, fm1);
-            op.store(i, r0, r1, v0, v1);
+            if (ft_in(J, i, i + 1, plane * g.nz, OOB_SWEEP_STORE)) op.store(i, r0, r1, v0, v1);
         }
         fm0 = fc0;
         fm1 = fc1;
@@ -452,12 +452,14 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         typename Op::Out r0{}, r1{};
         if (v0) r0 = op.apply(g, C, S, oc0, Pos{gx, gy, zs, bc0 + bczs}, fc0, fc1, left.b, up.a, dn.a, T(0), fm0);
         if (v1) r1 = op.apply(g, C, S, oc1, Pos{gx + 1, gy, zs, bc1 + bczs}, fc1, right.a, fc0, up.b, dn.b, T(0), fm1);
-        op.store(i_col + plane * zs, r0, r1, v0, v1);
+        const int64_t il = i_col + plane * zs;
+        if (ft_in(J, il, il + 1, plane * g.nz, OOB_SWEEP_STORE)) op.store(il, r0, r1, v0, v1);
     }
 
     using RT = typename RedType<Op>::type;
     RT v[NV];
     op.partials(v);
+    if (!ft_in(J, local * NPART, local * NPART + NPART - 1, J.ntiles * NPART, OOB_PARTIALS)) return SWEEP_FAULT;
     block_sum_store<NV, RT>(v, J.part + local * NPART, s_red);
     if (arrive_last(J.counter, J.ntiles, &s_flag)) {
         double tot[NV];

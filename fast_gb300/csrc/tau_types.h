@@ -79,7 +79,7 @@ struct Scalars {
     int32_t k1_mode;        // two-sweep BiCGSTAB: 1 = the next step 1 takes r from t (just replaced), e = 0;
                             // one-sweep CG: 1 = the next sweep restarts from the replaced residual
     int32_t cg_fused;       // 1: MIXED CG runs as one sweep per iteration (OpCGF)
-    int32_t pad_s;
+    int32_t oob;            // bounds-check builds: first failing access site (0 = none)
     // reductions for tau and porosity
     double flux_sum;    // sum over voxels of the tau flux term
     uint64_t pores;     // number of zero (pore) voxels
