@@ -583,15 +583,20 @@ def run_c4(args):
         out[str(rate)] = {"solves_per_s": len(done) / span, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                           "p99_ms": 1e3 * float(np.percentile(lat, 99)),
                           "all_converged": all(c.result.status == ft.Status.OK for c in done)}
-    # plain drop-in, one request per call (a bounded sample of the same stream)
-    nplain = min(len(masks), args.plain_sample)
+    # plain drop-in, one request per call, on the same requests (or, with
+    # --plain-sample n, on n of them evenly spaced through the stream so that
+    # the sample keeps the stream's size mix)
+    n = len(masks)
+    picks = list(range(n)) if args.plain_sample <= 0 or args.plain_sample >= n else \
+        sorted({int(i) for i in np.linspace(0, n - 1, args.plain_sample)})
     q = {s: ft.TortuosityParams(tolerance=1e-6, precision=ft.Precision.F64) for s in (0, 1)}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for k in range(nplain):
+    for k in picks:
         ft.solve_directions(masks[k], [ft.Dir(specs[k]["dir"])], q[specs[k]["solver"]],
                             ft.DiffusionSolverType(specs[k]["solver"]))
-    plain = nplain / (time.perf_counter() - t0)
+    plain = len(picks) / (time.perf_counter() - t0)
+    nplain = len(picks)
     best = max(v["solves_per_s"] for v in out.values())
     voxels = [m.size for m in masks]
     line = _line("tau solves/s", best, "solves/s", args, 1e3 / best, "f32+f64",
@@ -601,7 +606,8 @@ def run_c4(args):
                   "server": "TauServer MIXED, 16-iteration chunks, admission by HBM footprint"},
                  rates=out, plain_dropin_f64_solves_per_s=plain, plain_sample=nplain,
                  speedup_vs_plain_f64=best / plain,
-                 voxels_per_request={"mean": float(np.mean(voxels)), "max": int(max(voxels))})
+                 voxels_per_request={"mean": float(np.mean(voxels)), "max": int(max(voxels)),
+                                     "plain_sample_mean": float(np.mean([voxels[k] for k in picks]))})
     print(json.dumps(line), flush=True)
 
 
@@ -790,7 +796,8 @@ def main():
                     help="c2 (default) is the headline; the others print their own line")
     ap.add_argument("--requests", type=int, default=64, help="c4: requests in the stream")
     ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 2000.0], help="c4: arrival rates (1/s)")
-    ap.add_argument("--plain-sample", type=int, default=16, help="c4: requests timed on the plain solver")
+    ap.add_argument("--plain-sample", type=int, default=0,
+                    help="c4: requests timed on the plain solver (0: all of them)")
     ap.add_argument("--c5-edge", type=int, default=1024)
     ap.add_argument("--c5-no-reference", action="store_true")
     args = ap.parse_args()
