@@ -765,19 +765,28 @@ def run_alpha(args):
 
 def run_ncu_case(args):
     """A short, fixed run of the workload's kernels for profiler captures:
-    the bench volume, one direction (x), MIXED BiCGSTAB (or CG with
-    --ncu-solver cg) stopped after --ncu-iters iterations.  Prints the
-    iteration count; times nothing."""
+    the bench volume (the 64^3 plain drop-in volume with --workload c1),
+    one direction (x), BiCGSTAB (or CG with --ncu-solver cg) in MIXED (FP64
+    for c1, or --ncu-precision) stopped after --ncu-iters iterations.
+    Prints the iteration count; times nothing."""
     import torch
     import fast_gb300 as ft
-    w = WORKLOAD
-    mask = make_volume()
+    from fast_gb300 import volumes
+    if args.workload == "c1":
+        name = "c1_spheres64"
+        mask = volumes.spheres((64, 64, 64), seed=0, r_min=5.0, solid_fraction=0.60)
+        prec = args.ncu_precision or "f64"
+    else:
+        name = WORKLOAD["name"]
+        mask = make_volume()
+        prec = args.ncu_precision or "mixed"
     d_mask = torch.from_numpy(mask).cuda()
-    p = ft.TortuosityParams(tolerance=1e-12, max_iter=args.ncu_iters, precision=ft.Precision.MIXED)
+    p = ft.TortuosityParams(tolerance=1e-12, max_iter=args.ncu_iters, precision=ft.Precision[prec.upper()])
     solver = ft.DSOLVER_CG if args.ncu_solver == "cg" else ft.DSOLVER_BICGSTAB
     res = ft.solve_directions_device(d_mask.data_ptr(), mask.shape, [ft.Dir.X_POS], p, solver)
     torch.cuda.synchronize()
-    print(json.dumps({"ncu_case": w["name"] + "_x", "iterations": res[0].iterations, "status": int(res[0].status)}))
+    print(json.dumps({"ncu_case": name + "_x", "precision": prec, "iterations": res[0].iterations,
+                      "status": int(res[0].status)}))
 
 
 def main():
@@ -792,6 +801,7 @@ def main():
                     help="run a short fixed slice of the workload for profiler captures and exit")
     ap.add_argument("--ncu-iters", type=int, default=12)
     ap.add_argument("--ncu-solver", default="bicgstab", choices=["bicgstab", "cg"])
+    ap.add_argument("--ncu-precision", default=None, choices=["f64", "f32", "mixed"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "alpha"],
                     help="c2 (default) is the headline; the others print their own line")
     ap.add_argument("--requests", type=int, default=64, help="c4: requests in the stream")

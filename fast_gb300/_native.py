@@ -77,6 +77,9 @@ SIGNATURES = {
     "fast_porosity": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_double),
                                 C.POINTER(C.c_uint64)]),
     "fast_tau_last_stats": (C.c_int, [C.POINTER(fast_tau_stats)]),
+    "fast_tau_slab_depth": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "fast_tau_set_slab_table": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_int32]),
     "fast_porosity_device_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_uint64),
                                                C.POINTER(C.c_double), C.c_void_p]),
     "fast_tau_solve_batch": (C.c_int, [C.POINTER(fast_tau_volume), C.c_int32, C.POINTER(fast_tau_params),

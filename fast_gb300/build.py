@@ -37,6 +37,7 @@ def _nvcc() -> str:
 def _inputs():
     files = [os.path.join(CSRC, f) for f in CUDA_SOURCES + CXX_SOURCES + [CLI_SOURCE]]
     files += glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
+    files += glob.glob(os.path.join(CSRC, "*.inc"))
     files += glob.glob(os.path.join(INCLUDE, "*.h"))
     return files
 

@@ -38,8 +38,9 @@ constexpr int kSlabDepth = 32;   // planes per block (full size)
 constexpr int kMinBlocks = 608;  // 4 blocks per SM on 152 SMs
 // zc_req > 0: that slab depth; 0: FAST_TAU_ZC or kSlabDepth.
 Geometry make_geometry(int64_t nx, int64_t ny, int64_t nz, int zc_req = 0);
-// The slab depth of a volume's solves (size class; FAST_TAU_ZC overrides).
-int slab_depth(int64_t nx, int64_t ny, int64_t nz);
+// The slab depth of a volume solved alone with (precision, solver): the
+// tuned table of its size class; FAST_TAU_ZC overrides.
+int slab_depth(int64_t nx, int64_t ny, int64_t nz, int prec, int solver);
 size_t align_up(size_t v, size_t a);
 // Row pitch (elements) of every array of a volume: nx rounded up to 16, so a
 // row of any element size starts on a 16-byte boundary (TMA stride rule).

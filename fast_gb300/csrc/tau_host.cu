@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdarg>
@@ -421,33 +422,82 @@ struct JobSpec {
 
 size_t code_bytes(int64_t nx, int64_t ny, int64_t nz) { return align_up((size_t)(row_pitch(nx) * ny * nz), 256); }
 
-// Slab depth by size class: the full depth unless the launch would give the
-// GPU fewer than kMinBlocks blocks, then halved (down to 2 planes) until it
-// does.  A small volume otherwise runs as a few long z-marches (a 64^3 volume
-// makes 16 blocks of 32 planes) and is bound by the per-plane latency, not by
-// the work; a launch with many right-hand sides keeps the full depth (fewer
-// halo planes).  slab_depth sizes a volume solved alone (one right-hand side,
-// the serving context's unit); launch_slab_depth a whole launch.
-int slab_depth(int64_t nx, int64_t ny, int64_t nz)
+// Slab depth by size class.  A launch's size class is floor(log2(W)), W its
+// tile-planes: the sum over its right-hand sides of x tiles * y tiles * nz,
+// i.e. its block count at one plane per block.  Each (precision, solver,
+// class) has a depth: from the built-in table (slab_table.inc, written by
+// the autotuner, fast_gb300/autotune.py, from timings of a fixed number of
+// iterations at every candidate depth on a GB300), or from a table installed
+// at run time with fast_tau_set_slab_table.  A class without an entry uses
+// the full depth, halved (down to 2 planes) while the launch would give the
+// GPU fewer than kMinBlocks blocks.  FAST_TAU_ZC overrides all of it.
+// slab_depth sizes a volume solved alone (one right-hand side, the serving
+// context's unit, so a served result equals the same request solved alone);
+// launch_slab_depth a whole launch.
+#include "slab_table.inc"
+
+namespace {
+std::atomic<int> g_slab[3][2][kSlabClasses];
+std::once_flag g_slab_once;
+
+void slab_init()
 {
-    const int env = env_int("FAST_TAU_ZC", 0);
-    if (env > 0) return env;
-    int zc = kSlabDepth;
-    while (zc > 2 && make_geometry(nx, ny, nz, zc).ntiles < kMinBlocks) zc /= 2;
-    return zc;
+    std::call_once(g_slab_once, [] {
+        for (int p = 0; p < 3; p++)
+            for (int v = 0; v < 2; v++)
+                for (int c = 0; c < kSlabClasses; c++) g_slab[p][v][c].store(kSlabTable[p][v][c]);
+    });
 }
 
-int launch_slab_depth(const std::vector<VolSpec> &vols, const std::vector<JobSpec> &jobs)
+int slab_class(int64_t W)
+{
+    int c = 0;
+    while (c + 1 < kSlabClasses && (W >> (c + 1)) > 0) c++;
+    return c;
+}
+
+// The depth of a launch of right-hand sides with dimensions dims.
+int tuned_depth(int prec, int solver, const std::vector<const int64_t *> &dims)
 {
     const int env = env_int("FAST_TAU_ZC", 0);
     if (env > 0) return env;
+    int64_t W = 0;
+    for (const int64_t *d : dims) {
+        const Geometry G = make_geometry(d[0], d[1], d[2], 1);
+        W += (int64_t)G.tx * G.ty * d[2];
+    }
+    if (prec >= 0 && prec < 3 && solver >= 0 && solver < 2) {
+        slab_init();
+        const int t = g_slab[prec][solver][slab_class(W)].load(std::memory_order_relaxed);
+        if (t > 0) return t;
+    }
     int zc = kSlabDepth;
     for (; zc > 2; zc /= 2) {
         int64_t blocks = 0;
-        for (const JobSpec &j : jobs) blocks += make_geometry(vols[j.vol].nx, vols[j.vol].ny, vols[j.vol].nz, zc).ntiles;
+        for (const int64_t *d : dims) blocks += make_geometry(d[0], d[1], d[2], zc).ntiles;
         if (blocks >= kMinBlocks) break;
     }
     return zc;
+}
+}  // namespace
+
+int slab_depth(int64_t nx, int64_t ny, int64_t nz, int prec, int solver)
+{
+    const int64_t d[3] = {nx, ny, nz};
+    return tuned_depth(prec, solver, {d});
+}
+
+int launch_slab_depth(const std::vector<VolSpec> &vols, const std::vector<JobSpec> &jobs, int prec, int solver)
+{
+    std::vector<const int64_t *> dims;
+    std::vector<int64_t> flat(3 * vols.size());
+    for (size_t v = 0; v < vols.size(); v++) {
+        flat[3 * v] = vols[v].nx;
+        flat[3 * v + 1] = vols[v].ny;
+        flat[3 * v + 2] = vols[v].nz;
+    }
+    for (const JobSpec &j : jobs) dims.push_back(&flat[3 * j.vol]);
+    return tuned_depth(prec, solver, dims);
 }
 
 // The one-sweep MIXED CG (OpCGF) is opt-in (FAST_TAU_CG_FUSED=1): its
@@ -472,7 +522,7 @@ size_t job_bytes(int64_t nx, int64_t ny, int64_t nz, int prec, int solver, int z
     const bool fused = mixed && solver == FAST_SOLVER_CG && cg_fused_enabled();
     const size_t nvec = (solver == FAST_SOLVER_CG && !fused) ? 4 : (mixed ? 9 : 8);
     const size_t NP = (size_t)(row_pitch(nx) * ny * nz);
-    const Geometry G = make_geometry(nx, ny, nz, zc > 0 ? zc : slab_depth(nx, ny, nz));
+    const Geometry G = make_geometry(nx, ny, nz, zc > 0 ? zc : slab_depth(nx, ny, nz, prec, solver));
     return nvec * align_up(NP * vec_t, 256) + (mixed ? 2 * align_up(NP * 8, 256) : 0) +
            align_up((size_t)G.ntiles * NPART * sizeof(double), 256);
 }
@@ -496,7 +546,7 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     const int prec = P.precision, solver = P.solver;
     const bool mixed = prec == FAST_PREC_MIXED;
     const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
-    const Geometry G = make_geometry(nx, ny, nz, zc > 0 ? zc : slab_depth(nx, ny, nz));
+    const Geometry G = make_geometry(nx, ny, nz, zc > 0 ? zc : slab_depth(nx, ny, nz, prec, solver));
     const int64_t pitch = row_pitch(nx);
     const int64_t NP = pitch * ny * nz;
     const size_t vbytes = align_up((size_t)NP * vec_t, 256);
@@ -592,7 +642,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     const size_t vec_t = (prec == FAST_PREC_F64) ? 8 : 4;
 
     // --- memory plan (the reference's fit check, VolumeMeasures.cpp:104-125)
-    const int zc = launch_slab_depth(vols, jobs);
+    const int zc = launch_slab_depth(vols, jobs, prec, solver);
     const size_t need = solve_bytes(vols, jobs, prec, solver, zc);
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
@@ -836,6 +886,40 @@ extern "C" {
 FAST_API const char *fast_last_error(void) { return g_last_error.c_str(); }
 
 FAST_API const char *fast_version(void) { return "fasttau 0.1 (sm_103a)"; }
+
+FAST_API int fast_tau_slab_depth(int64_t nx, int64_t ny, int64_t nz, int32_t nrhs, int32_t precision,
+                                 int32_t solver, int32_t *depth, int32_t *size_class)
+{
+    ft_clear_error();
+    if (!depth) return fail(FAST_BAD_ARG, "depth is NULL");
+    if (nx < 1 || ny < 1 || nz < 1 || nrhs < 1 || nrhs > 6) return fail(FAST_BAD_ARG, "bad dimensions or nrhs");
+    if (precision < FAST_PREC_F64 || precision > FAST_PREC_MIXED) return fail(FAST_BAD_ARG, "bad precision");
+    if (solver != FAST_SOLVER_BICGSTAB && solver != FAST_SOLVER_CG) return fail(FAST_BAD_ARG, "bad solver");
+    const int64_t d[3] = {nx, ny, nz};
+    const std::vector<const int64_t *> dims((size_t)nrhs, d);
+    *depth = std::min<int64_t>(tuned_depth(precision, solver, dims), nz);
+    if (size_class) {
+        const Geometry G = make_geometry(nx, ny, nz, 1);
+        *size_class = slab_class((int64_t)G.tx * G.ty * nz * nrhs);
+    }
+    return FAST_OK;
+}
+
+FAST_API int fast_tau_set_slab_table(int32_t precision, int32_t solver, const int32_t *depth_by_class, int32_t nclass)
+{
+    ft_clear_error();
+    if (precision < FAST_PREC_F64 || precision > FAST_PREC_MIXED) return fail(FAST_BAD_ARG, "bad precision");
+    if (solver != FAST_SOLVER_BICGSTAB && solver != FAST_SOLVER_CG) return fail(FAST_BAD_ARG, "bad solver");
+    if (nclass < 0 || nclass > kSlabClasses) return fail(FAST_BAD_ARG, "0..%d classes", kSlabClasses);
+    if (nclass > 0 && !depth_by_class) return fail(FAST_BAD_ARG, "depth_by_class is NULL");
+    for (int c = 0; c < nclass; c++)
+        if (depth_by_class[c] < 0 || depth_by_class[c] > 1024) return fail(FAST_BAD_ARG, "depth out of range");
+    slab_init();
+    for (int c = 0; c < kSlabClasses; c++)
+        g_slab[precision][solver][c].store(!depth_by_class ? kSlabTable[precision][solver][c]
+                                                           : (c < nclass ? depth_by_class[c] : 0));
+    return FAST_OK;
+}
 
 FAST_API int fast_tau_last_stats(fast_tau_stats *out)
 {

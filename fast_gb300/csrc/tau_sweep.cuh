@@ -360,17 +360,7 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         const int zq = pa + q;
         const int st = (qb + q) % NSTAGE;
         const uint32_t par = (uint32_t)(((qb + q) / NSTAGE) & 1);
-#if FAST_TAU_WAIT_WARP0
-        // Warp 0 waits for the stage; the other warps sleep in the barrier
-        // instead of spinning on the mbarrier, then observe the completed
-        // phase once.
-        if (tid < 32 && !mbar_wait_bounded(smem_u32(&bars[st]), par)) s_err = 1;
-        __syncthreads();
-        if (s_err) break;
-        if (tid >= 32) (void)mbar_try_wait(smem_u32(&bars[st]), par);
-#else
         if (!mbar_wait_bounded<WaitHint<Op>::ns>(smem_u32(&bars[st]), par)) s_err = 1;
-#endif
         const unsigned char *stage = sbase + st * SB;
         const bool out_plane = zq >= z0 && zq < z1;
         const int bcz = boundary_count_z(g, zq);

@@ -230,6 +230,21 @@ typedef struct fast_tau_stats {
 
 FAST_API int fast_tau_last_stats(fast_tau_stats *out);
 
+/* Slab depth (z planes per block of the solver sweeps) by size class.  No
+ * reference counterpart: the reference launches one thread per voxel.  A
+ * launch's class is floor(log2(W)), W = the sum over its right-hand sides of
+ * ceil(nx/64) * ceil(ny/8) * nz.  fast_tau_slab_depth gives the depth a solve
+ * of nrhs right-hand sides of an nx x ny x nz volume would use (the
+ * FAST_TAU_ZC environment variable overrides the table).
+ * fast_tau_set_slab_table installs the depths of one (precision, solver) for
+ * classes 0..nclass-1 (0 = no entry: the full depth, halved while the launch
+ * has fewer than 608 blocks); depth_by_class NULL restores the built-in
+ * table, which fast_gb300/autotune.py writes from GB300 timings. */
+FAST_API int fast_tau_slab_depth(int64_t nx, int64_t ny, int64_t nz, int32_t nrhs, int32_t precision,
+                                 int32_t solver, int32_t *depth, int32_t *size_class /* nullable */);
+FAST_API int fast_tau_set_slab_table(int32_t precision, int32_t solver, const int32_t *depth_by_class,
+                                     int32_t nclass);
+
 /* Pore count of a DEVICE-resident mask that allocates nothing, for callers
  * that cannot allocate device memory: code running while a stream is being
  * captured into a CUDA graph, or an application whose device memory is owned

@@ -3,8 +3,8 @@ store of the solver kernels checks its index, records the first failing site
 in the right-hand side's scalars and skips the access; the call then fails
 with "bounds check".  This test builds that variant of the library, runs the
 awkward shapes (one-voxel axes, a one-plane primary axis, sizes that are not
-tile multiples) in every direction, precision and solver, and batches of
-mixed sizes through it in a child process, and requires that no access was
+tile multiples) in every direction, precision and solver, slab depths of 3
+and 64 planes, and batches of mixed sizes through it in a child process, and requires that no access was
 out of range and the results equal the regular build's."""
 import json
 import os
@@ -36,6 +36,22 @@ for s in shapes:
                 except Exception as e:
                     tau, err = 0.0, str(e)
                 out.append([list(s), d, int(prec), int(solver), tau, err])
+import os
+for zc in ("3", "64"):
+    os.environ["FAST_TAU_ZC"] = zc
+    for s in [(70, 9, 33), (130, 20, 17)]:
+        m = volumes.spheres(s, 3, 1.0, 2.0, 0.3)
+        for d in (0, 5):
+            for prec in (ft.Precision.F64, ft.Precision.MIXED):
+                for solver in (ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB):
+                    p = ft.TortuosityParams(dir=ft.Dir(d), tolerance=1e-6, precision=prec)
+                    try:
+                        tau = ft.get_tortuosity(m, p, solver)
+                        err = ""
+                    except Exception as e:
+                        tau, err = 0.0, str(e)
+                    out.append(["zc" + zc, list(s), d, int(prec), int(solver), tau, err])
+os.environ.pop("FAST_TAU_ZC", None)
 vols = [volumes.spheres(s, 5, 1.0, 2.0, 0.35) for s in [(9, 33, 17), (40, 8, 3), (16, 16, 16)]]
 p = ft.TortuosityParams(tolerance=1e-6, precision=ft.Precision.MIXED)
 res = ft.solve_batch(list(zip(vols, [ft.Dir.X_POS, ft.Dir.Y_NEG, ft.Dir.Z_POS])), p, ft.DSOLVER_CG)

@@ -137,6 +137,41 @@ def test_known_answers(gpu):
     assert rel(ft.get_tortuosity(m, p, ft.DSOLVER_CG), phi / (phi + (1 - phi) * d1)) < 1e-9
 
 
+@pytest.mark.parametrize("zc", [3, 64, 1000])
+def test_slab_depths_match_oracle(gpu, oracle, monkeypatch, zc):
+    """Any slab depth (an odd one, the tuner's largest candidate, one above
+    the volume's planes) gives the oracle's tau in every precision: the
+    depth changes only the summation order of the partial sums."""
+    monkeypatch.setenv("FAST_TAU_ZC", str(zc))
+    mask = _vol((70, 19, 33), seed=29)
+    for d in (0, 4, 5):
+        ref = oracle.get_tortuosity(mask, dir=d, solver=1, tol=1e-10)
+        assert ref["status"] == 0
+        for solver in (ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB):
+            for prec, bound in ((ft.Precision.F64, 1e-8), (ft.Precision.MIXED, 1e-5)):
+                tol = 1e-10 if prec == ft.Precision.F64 else 1e-7
+                p = ft.TortuosityParams(dir=ft.Dir(d), tolerance=tol, precision=prec)
+                tau = ft.get_tortuosity(mask, p, solver)
+                assert rel(tau, ref["tau"]) <= bound, (zc, d, solver, prec, tau, ref["tau"])
+
+
+def test_tuned_depths_match_oracle(gpu, oracle, monkeypatch):
+    """Volumes whose size classes select different tuned depths (2 to 64
+    planes) match the oracle with the built-in table."""
+    monkeypatch.delenv("FAST_TAU_ZC", raising=False)
+    from fast_gb300 import autotune as at
+    seen = set()
+    for shape in ((40, 40, 40), (128, 64, 64), (256, 64, 64)):
+        mask = _vol(shape, seed=sum(shape))
+        ref = oracle.get_tortuosity(mask, dir=0, solver=1, tol=1e-10)
+        for solver in (ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB):
+            seen.add(at.slab_depth(shape, 1, ft.Precision.MIXED, solver)[0])
+            p = ft.TortuosityParams(dir=ft.Dir.X_POS, tolerance=1e-7, precision=ft.Precision.MIXED)
+            tau = ft.get_tortuosity(mask, p, solver)
+            assert rel(tau, ref["tau"]) <= 1e-5, (shape, solver, tau, ref["tau"])
+    assert len(seen) >= 2
+
+
 @pytest.mark.parametrize("shape", [(1, 1, 1), (1, 5, 1), (3, 1, 1), (1, 1, 7), (2, 3, 1), (33, 9, 65)])
 def test_edge_shapes(gpu, oracle, shape):
     rng = np.random.default_rng(sum(shape))
