@@ -34,12 +34,13 @@ from typing import Dict, List, Optional, Sequence, Tuple
 from . import _native
 from .tau import DiffusionSolverType, Dir, Precision, TortuosityParams, solve_directions
 
-CANDIDATES = (2, 4, 8, 16, 32, 64)
+CANDIDATES = (2, 4, 8, 16, 32, 64, 128, 256)
+DEVICE_TIMED_S = 2e-3  # iterations longer than this are timed by their kernels' events
 NUM_CLASSES = 32
 # (edge, right-hand sides): cubes across the sizes the engine serves, plus
 # the three-direction launches of the batched and benchmark workloads.
 DEFAULT_CASES = ((32, 1), (48, 1), (64, 1), (80, 1), (96, 1), (128, 1), (160, 1), (192, 1), (224, 1),
-                 (256, 1), (320, 1), (384, 1), (64, 3), (128, 3), (256, 3))
+                 (256, 1), (320, 1), (384, 1), (512, 1), (64, 3), (128, 3), (256, 3))
 PRECISIONS = (Precision.F64, Precision.F32, Precision.MIXED)
 SOLVERS = (DiffusionSolverType.DSOLVER_BICGSTAB, DiffusionSolverType.DSOLVER_CG)
 TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "slab_table.inc")
@@ -97,6 +98,35 @@ def _timed(mask, dirs, prec, solver, iters) -> Tuple[float, bool]:
     return dt, all(r.iterations >= iters for r in res)
 
 
+_SETUP_KERNELS = ("code", "init", "init64", "tau")
+
+
+def _per_iteration_device(mask, dirs, prec, solver, depth, iters, repeats) -> Optional[float]:
+    """Seconds per iteration from the library's per-kernel CUDA-event
+    profile (the iteration kernels only), for launches whose iterations are
+    long enough that the event bracketing of every launch costs nothing
+    measurable while the allocation of their state would swamp a wall-clock
+    difference."""
+    old = os.environ.get("FAST_TAU_ZC")
+    os.environ["FAST_TAU_ZC"] = str(depth)
+    try:
+        p = TortuosityParams(tolerance=1e-30, max_iter=iters, precision=prec, profile=True)
+        best = None
+        for _ in range(repeats + 1):  # the first solve warms up
+            res = solve_directions(mask, dirs, p, solver)
+            if not all(r.iterations >= iters for r in res):
+                return None
+            ks = _native.last_stats()["kernels"]
+            v = sum(k["ms"] for name, k in ks.items() if name not in _SETUP_KERNELS) / 1e3 / iters
+            best = v if best is None else min(best, v)
+        return best
+    finally:
+        if old is None:
+            os.environ.pop("FAST_TAU_ZC", None)
+        else:
+            os.environ["FAST_TAU_ZC"] = old
+
+
 def _per_iteration(mask, dirs, prec, solver, depth, base_iters, span, repeats) -> Optional[float]:
     """Seconds per iteration of the launch at this depth (None if a solve
     stopped early)."""
@@ -125,7 +155,9 @@ def measure(cases: Sequence[Tuple[int, int]] = DEFAULT_CASES, precisions: Sequen
             repeats: int = 2, target_s: float = 0.03, log=None) -> List[dict]:
     """Per-iteration times of every case, precision, solver and candidate
     depth (depths above the volume's planes are skipped).  The iteration
-    span of a case is sized so that it runs about target_s seconds."""
+    span of a case is sized so that it runs about target_s seconds.  Where
+    an iteration takes more than DEVICE_TIMED_S the time is the kernels'
+    own (CUDA events), else the wall-clock difference of two solves."""
     rows = []
     for edge, nrhs in cases:
         mask = _volume(edge, seed=1000 + edge)
@@ -133,17 +165,22 @@ def measure(cases: Sequence[Tuple[int, int]] = DEFAULT_CASES, precisions: Sequen
         for prec in precisions:
             for solver in solvers:
                 _, cls = slab_depth(mask.shape, nrhs, prec, solver)
-                # size the span from one probe at the current depth
-                probe = _per_iteration(mask, dirs, prec, solver, slab_depth(mask.shape, nrhs, prec, solver)[0],
-                                       8, 16, 1)
+                # size the span from one kernel-timed probe at the current depth
+                probe = _per_iteration_device(mask, dirs, prec, solver,
+                                              slab_depth(mask.shape, nrhs, prec, solver)[0], 16, 1)
                 span = 64 if not probe else int(min(2000, max(16, target_s / probe)))
+                device = bool(probe) and probe > DEVICE_TIMED_S
                 times = {}
                 for d in candidates:
                     if d > edge:
                         continue
-                    times[d] = _per_iteration(mask, dirs, prec, solver, d, 8, span, repeats)
+                    if device:
+                        times[d] = _per_iteration_device(mask, dirs, prec, solver, d, span, repeats)
+                    else:
+                        times[d] = _per_iteration(mask, dirs, prec, solver, d, 8, span, repeats)
                 row = {"edge": edge, "nrhs": nrhs, "precision": prec.name, "solver": int(solver), "class": cls,
                        "voxels": edge ** 3 * nrhs, "span": span, "s_per_iter": times,
+                       "timing": "kernel events" if device else "wall-clock difference",
                        "rule_depth": rule_depth(mask.shape, nrhs, prec, solver)}
                 rows.append(row)
                 if log:
@@ -152,8 +189,9 @@ def measure(cases: Sequence[Tuple[int, int]] = DEFAULT_CASES, precisions: Sequen
 
 
 def table_from(rows: Sequence[dict], tolerance: float = 0.02) -> Dict[Tuple[str, int], List[int]]:
-    """Depth per class for every (precision, solver) in rows: the depth of
-    least pooled time per voxel-iteration, unless a depth the block-count
+    """Depth per class for every (precision, solver) in rows: of the depths
+    measured in every case of the class, the one of least pooled time per
+    voxel-iteration, unless a depth the block-count
     rule gives the class's cases is within `tolerance` of it (then that
     one: a change needs a gain above the timing noise); nearest measured
     class for the rest."""
@@ -177,7 +215,10 @@ def table_from(rows: Sequence[dict], tolerance: float = 0.02) -> Dict[Tuple[str,
                     acc[d] = acc.get(d, 0.0) + t / r["voxels"]
         best = {}
         for c, acc in pooled.items():
-            ok = {d: t for d, t in acc.items() if d not in bad.get(c, set())}
+            # only depths measured in every case of the class compare fairly
+            cases = [r for r in rows if (r["precision"], r["solver"]) == key and r["class"] == c]
+            common = set.intersection(*[{int(d) for d in r["s_per_iter"]} for r in cases])
+            ok = {d: t for d, t in acc.items() if d in common and d not in bad.get(c, set())}
             if ok:
                 fastest = min(ok, key=ok.get)
                 near = [d for d in rule.get(c, ()) if d in ok and ok[d] <= ok[fastest] * (1.0 + tolerance)]
@@ -239,7 +280,9 @@ def main(argv=None) -> int:
     ap.add_argument("--repeats", type=int, default=2)
     ap.add_argument("--target-s", type=float, default=0.03, help="seconds of iterations per timed span")
     ap.add_argument("--json", default=None, help="write the raw timings here")
-    ap.add_argument("--from-json", default=None, help="build the table from timings written by --json")
+    ap.add_argument("--from-json", default=None,
+                    help="build the table from timings written by --json (comma list: a later file's rows "
+                         "replace an earlier file's rows of the same case, precision and solver)")
     ap.add_argument("--tolerance", type=float, default=0.02,
                     help="keep the block-count rule's depth when within this fraction of the fastest")
     ap.add_argument("--install", action="store_true", help="use the measured table in this process")
@@ -251,9 +294,14 @@ def main(argv=None) -> int:
     solvers = SOLVERS if not a.solvers else [DiffusionSolverType["DSOLVER_" + v] for v in a.solvers.split(",")]
     device = _device_name()
     if a.from_json:
-        with open(a.from_json) as f:
-            saved = json.load(f)
-        rows, device = saved["rows"], saved.get("device", device)
+        merged = {}
+        for path in a.from_json.split(","):
+            with open(path) as f:
+                saved = json.load(f)
+            device = saved.get("device", device)
+            for r in saved["rows"]:
+                merged[(r["edge"], r["nrhs"], r["precision"], r["solver"])] = r
+        rows = list(merged.values())
         for r in rows:
             if "rule_depth" not in r:
                 r["rule_depth"] = rule_depth((r["edge"],) * 3, r["nrhs"], Precision[r["precision"]],

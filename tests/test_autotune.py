@@ -83,6 +83,14 @@ def test_table_from_pools_cases_and_fills_gaps():
     assert len(t) == at.NUM_CLASSES
     assert t[9] == 4 and t[12] == 16
     assert t[0] == 4 and t[10] == 4 and t[11] == 16 and t[31] == 16  # nearest measured class
+    # a depth measured in only one case of a class does not compete
+    rows.append({"precision": "MIXED", "solver": 1, "class": 12, "voxels": 10, "s_per_iter": {16: 2e-3, 64: 1e-4}})
+    assert at.table_from(rows)[("MIXED", 1)][12] == 16
+    # the block-count rule's depth stays when within the tolerance of the fastest
+    near = [{"precision": "F32", "solver": 0, "class": 15, "voxels": 1, "rule_depth": 32,
+             "s_per_iter": {16: 1.00, 32: 1.015, 64: 1.05}}]
+    assert at.table_from(near)[("F32", 0)][15] == 32
+    assert at.table_from(near, tolerance=0.01)[("F32", 0)][15] == 16
 
 
 def test_render_round_trips_and_committed_header_is_well_formed():
