@@ -19,11 +19,17 @@
 //      voxel's x-run (ballot + count-leading-zeros over 32-voxel chunks);
 //   2. union: each foreground voxel joins its y-1 and z-1 neighbours, skipping
 //      a join already implied through the x-1 voxel (both x-1 voxels
-//      foreground); atomicMin linking, lock-free;
-//   3. flatten: parent[i] = root;
-//   4. count roots per 8192-voxel chunk, 5. scan the chunk counts,
-//   6. rank the roots, 7. labels[i] = rank of root(i);
-//   8. face bitmaps, 9. the all-faces AND.
+//      foreground); Rem's union with splicing, lock-free (compare-and-swap).
+//      Every stored parent is a run start, so afterwards a voxel points at
+//      a run start (its own or one joined to it);
+//   3. starts: one warp per row; every run start that is a root counts
+//      itself in its 8192-voxel chunk and sets its bit of a root bitmap,
+//      every other run start is pointed straight at its root;
+//   4. scan the chunk counts;
+//   5. rank: one block per chunk numbers the chunk's roots from the bitmap;
+//   6. relabel: labels[i] = label of parent[parent[i]] (the root: the run
+//      start's parent), 0 on the background;
+//   7. face bitmaps, 8. the all-faces AND.
 // Every loop terminates: a find follows strictly decreasing indices, and a
 // failed link continues from a strictly smaller index.
 #include <cuda_runtime.h>
@@ -37,10 +43,21 @@ namespace {
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;  // parent of a background voxel
 constexpr int kChunk = 8192;             // voxels per block in the ranking passes
-constexpr int kRankThreads = 256;        // 32 consecutive voxels per thread
+constexpr int kRankThreads = 256;        // one root-bitmap word (32 voxels) per thread
+static_assert(kChunk == kRankThreads * 32, "a rank block covers one chunk");
 
-__device__ __forceinline__ uint32_t ld_par(const uint32_t *p, uint32_t i) { return __ldcg(p + i); }
+// Parent reads during the union and starts passes go through L1
+// (ld.global.ca): a read may return a stale parent written earlier in the
+// same pass by another SM, which is harmless.  Every value ever stored is a
+// pointer to a smaller index of the same component, so a walk that follows
+// stale pointers still ends at a root.  A stale "root" is caught by the
+// linking compare-and-swap, whose old value the union continues from.  The next
+// pass, after the kernel boundary, sees the final values.  The root of a
+// large component is read by most finds; through L2 alone that one line
+// would serialise them.
+__device__ __forceinline__ uint32_t ld_par(const uint32_t *p, uint32_t i) { return __ldca(p + i); }
 
+// Root of a's tree (no writes).
 __device__ __forceinline__ uint32_t find_root(const uint32_t *par, uint32_t a)
 {
     uint32_t p = ld_par(par, a);
@@ -51,22 +68,41 @@ __device__ __forceinline__ uint32_t find_root(const uint32_t *par, uint32_t a)
     return a;
 }
 
-__device__ void unite(uint32_t *par, uint32_t a, uint32_t b)
+// Joins the trees of x and y: Rem's union with splicing, concurrent form
+// (links by compare-and-swap).  The node whose parent is larger moves up;
+// before it does, its parent is swung to the other node's (smaller) parent,
+// so paths shorten as unions proceed; the walk stops as soon as both nodes
+// have the same parent, which for two voxels already in one component
+// usually happens well below the root.  Invariants: a parent never exceeds
+// its node (so a root is its tree's smallest index) and every stored parent
+// is a run start (a voxel inside a run is never anyone's parent), which the
+// starts and relabel passes rely on.  A link or splice that loses a race
+// only fails its compare-and-swap; a failed link hands back the node's
+// current parent, so a stale read cannot make the loop spin, and every
+// step moves a node to a strictly smaller index.
+__device__ void unite(uint32_t *par, uint32_t x, uint32_t y)
 {
+    uint32_t px = ld_par(par, x), py = ld_par(par, y);
     for (;;) {
-        a = find_root(par, a);
-        b = find_root(par, b);
-        if (a == b) return;
-        if (a < b) {
-            const uint32_t t = a;
-            a = b;
-            b = t;
+        if (px == py) return;
+        if (px < py) {
+            uint32_t t = x;
+            x = y;
+            y = t;
+            t = px;
+            px = py;
+            py = t;
         }
-        // a > b: hang a's tree under b.  If a stopped being a root meanwhile,
-        // continue with its new parent (smaller than a).
-        const uint32_t old = atomicMin(par + a, b);
-        if (old == a) return;
-        a = old;
+        // px > py
+        if (x == px) {  // x is a root: hang it under y's parent
+            const uint32_t old = atomicCAS(par + x, x, py);
+            if (old == x) return;
+            px = old;  // x got a parent meanwhile
+            continue;
+        }
+        atomicCAS(par + x, px, py);  // splice; losing the race is harmless
+        x = px;
+        px = ld_par(par, x);
     }
 }
 
@@ -111,26 +147,35 @@ __global__ void ccl_union(const uint8_t *__restrict__ m, uint32_t *par, int nx, 
     }
 }
 
-// Pass 3: parent[i] = root for every foreground voxel.
-__global__ void ccl_flatten(uint32_t *par, uint32_t n)
+// Pass 3: run starts.  A root (a start whose parent is itself) counts
+// itself in its chunk and sets its bit in the root bitmap; another start
+// gets its root as parent.  The other voxels of a run keep the start.
+__global__ void ccl_starts(const uint8_t *__restrict__ m, uint32_t *par, int nx, int64_t rows, uint8_t bg,
+                           uint32_t *chunk_cnt, uint32_t *root_bits)
 {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = ld_par(par, i);
-        if (p == kNone || p == i) continue;
-        par[i] = find_root(par, p);
+    const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (row >= rows) return;
+    const int lane = threadIdx.x & 31;
+    const uint32_t base = (uint32_t)(row * nx);
+    bool carry = false;  // voxel x0 - 1 is foreground
+    for (int x0 = 0; x0 < nx; x0 += 32) {
+        const int x = x0 + lane;
+        const bool fg = x < nx && m[base + x] != bg;
+        const unsigned fgm = __ballot_sync(0xFFFFFFFFu, fg);
+        const bool prev = lane == 0 ? carry : ((fgm >> (lane - 1)) & 1u) != 0;
+        carry = (fgm >> 31) & 1u;
+        if (fg && !prev) {
+            const uint32_t i = base + (uint32_t)x;
+            const uint32_t p = ld_par(par, i);
+            if (p == i) {
+                atomicAdd(chunk_cnt + i / (uint32_t)kChunk, 1u);
+                atomicOr(root_bits + (i >> 5), 1u << (i & 31u));
+            } else {
+                const uint32_t r = find_root(par, p);
+                if (r != p) par[i] = r;
+            }
+        }
     }
-}
-
-// Roots among a thread's 32 consecutive voxels of a chunk.
-__device__ __forceinline__ uint32_t root_bits(const uint32_t *par, uint32_t first, uint32_t n)
-{
-    uint32_t bits = 0;
-#pragma unroll 8
-    for (int k = 0; k < 32; k++) {
-        const uint32_t i = first + (uint32_t)k;
-        if (i < n && ld_par(par, i) == i) bits |= 1u << k;
-    }
-    return bits;
 }
 
 // Exclusive block scan of one value per thread (kRankThreads threads).
@@ -161,18 +206,7 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s
     return s_warp[w] + inc - v;
 }
 
-// Pass 4: roots per chunk.
-__global__ void __launch_bounds__(kRankThreads) ccl_count(const uint32_t *par, uint32_t n, uint32_t *chunk_cnt)
-{
-    __shared__ uint32_t s_warp[kRankThreads / 32 + 1];
-    const uint32_t first = blockIdx.x * (uint32_t)kChunk + threadIdx.x * 32u;
-    const uint32_t c = (uint32_t)__popc(root_bits(par, first, n));
-    uint32_t total;
-    block_exclusive_scan(c, s_warp, total);
-    if (threadIdx.x == 0) chunk_cnt[blockIdx.x] = total;
-}
-
-// Pass 5: exclusive scan of the chunk counts in place (one block of 1024
+// Pass 4: exclusive scan of the chunk counts in place (one block of 1024
 // threads, each summing a contiguous slice); cnt[nchunks] = number of roots.
 __global__ void __launch_bounds__(1024) ccl_scan_chunks(uint32_t *cnt, uint32_t nchunks)
 {
@@ -198,33 +232,59 @@ __global__ void __launch_bounds__(1024) ccl_scan_chunks(uint32_t *cnt, uint32_t 
     if (threadIdx.x == 1023) cnt[nchunks] = s[1023];
 }
 
-// Pass 6: label of every root = 1 + its rank; background voxels get 0.
-__global__ void __launch_bounds__(kRankThreads) ccl_rank(const uint32_t *par, uint32_t n, const uint32_t *chunk_off,
-                                                         uint32_t *labels)
+// Pass 5: label of every root = 1 + its rank.  One block per chunk, one
+// bitmap word (32 voxels) per thread.
+__global__ void __launch_bounds__(kRankThreads) ccl_rank(const uint32_t *__restrict__ root_bits, uint32_t nwords,
+                                                         const uint32_t *__restrict__ chunk_off, uint32_t *labels)
 {
     __shared__ uint32_t s_warp[kRankThreads / 32 + 1];
-    const uint32_t first = blockIdx.x * (uint32_t)kChunk + threadIdx.x * 32u;
-    const uint32_t bits = root_bits(par, first, n);
+    const uint32_t w = blockIdx.x * (uint32_t)kRankThreads + threadIdx.x;
+    uint32_t bits = w < nwords ? root_bits[w] : 0u;
     uint32_t total;
     uint32_t r = chunk_off[blockIdx.x] + block_exclusive_scan((uint32_t)__popc(bits), s_warp, total) + 1u;
-    for (int k = 0; k < 32; k++) {
-        const uint32_t i = first + (uint32_t)k;
-        if (i >= n) break;
-        if (bits & (1u << k)) labels[i] = r++;
-        else if (ld_par(par, i) == kNone) labels[i] = 0u;
+    while (bits) {
+        const uint32_t k = (uint32_t)(__ffs(bits) - 1);
+        labels[w * 32u + k] = r++;
+        bits &= bits - 1u;
     }
 }
 
-// Pass 7: every other foreground voxel takes its root's label.
-__global__ void ccl_relabel(const uint32_t *par, uint32_t n, uint32_t *labels)
+// Pass 6: every other voxel: 0 on the background, else the label of its
+// root, which is its parent's parent (a run start points at its root, a
+// root at itself).  Roots were labelled by pass 5 and are not written here.
+// Four voxels a thread per step, their loads issued together.  A root's
+// label is read through the non-coherent L1 path: one component can own
+// most of the volume, and its root's label, read by every one of its
+// voxels, would otherwise be one L2 line hit by every SM.  Root entries
+// were written by the rank pass and are not written here (only non-root
+// entries are), so the cached values are current.
+__global__ void ccl_relabel(const uint32_t *__restrict__ par, uint32_t n, uint32_t *labels)
 {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = ld_par(par, i);
-        if (p != kNone && p != i) labels[i] = __ldcg(labels + p);
+    constexpr int U = 4;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += U * stride) {
+        uint32_t p[U], r[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint64_t i = i0 + u * stride;
+            p[u] = i < n ? __ldg(par + i) : kNone;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint64_t i = i0 + u * stride;
+            r[u] = (p[u] != kNone && p[u] != i) ? __ldg(par + p[u]) : kNone;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint64_t i = i0 + u * stride;
+            if (i >= n) break;
+            if (p[u] == kNone) labels[i] = 0u;
+            else if (r[u] != kNone) labels[i] = __ldg(labels + r[u]);
+        }
     }
 }
 
-// Pass 8: the six face bitmaps.  Face d (Dir order) of the volume, flattened
+// Pass 7: the six face bitmaps.  Face d (Dir order) of the volume, flattened
 // over the two secondary axes; faces are concatenated in d order.
 __global__ void ccl_faces(const uint32_t *labels, int nx, int ny, int nz, uint32_t num_labels, uint8_t *bnd)
 {
@@ -250,7 +310,7 @@ __global__ void ccl_faces(const uint32_t *labels, int nx, int ny, int nz, uint32
     }
 }
 
-// Pass 9: row 6 = AND of rows 0..5.
+// Pass 8: row 6 = AND of rows 0..5.
 __global__ void ccl_all_faces(uint32_t num_labels, uint8_t *bnd)
 {
     for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < num_labels; l += gridDim.x * blockDim.x) {
@@ -275,27 +335,35 @@ int check_dims(int64_t nx, int64_t ny, int64_t nz)
     return FAST_OK;
 }
 
+// Scratch words of a labelling beside the parent array: the chunk counts
+// (nchunks + 1) and the root bitmap (one bit per voxel).
+size_t scratch_words(uint32_t n)
+{
+    const size_t nchunks = (n + kChunk - 1) / kChunk;
+    return nchunks + 1 + nchunks * (kChunk / 32);
+}
+
 // Labels of d_mask into d_labels (device, N uint32) on `st`, using d_par
-// (device, N uint32) and d_cnt (device, nchunks + 1 uint32) as scratch.
+// (device, N uint32) and d_scr (device, scratch_words(N) uint32) as scratch.
 int label_device(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, uint8_t bg, uint32_t *d_labels,
-                 uint32_t *d_par, uint32_t *d_cnt, uint32_t *num_labels, cudaStream_t st)
+                 uint32_t *d_par, uint32_t *d_scr, uint32_t *num_labels, cudaStream_t st)
 {
     const uint32_t n = (uint32_t)(nx * ny * nz);
     const int64_t rows = ny * nz;
+    const uint32_t nchunks = (n + kChunk - 1) / kChunk;
+    uint32_t *d_cnt = d_scr, *d_bits = d_scr + nchunks + 1;
+    CK(cudaMemsetAsync(d_scr, 0, scratch_words(n) * 4, st));
     ccl_rows<<<(unsigned)((rows + 7) / 8), 256, 0, st>>>(d_mask, d_par, (int)nx, rows, bg);
     const dim3 ub(32, 8, 1);
     const dim3 ug((unsigned)((nx + 31) / 32), (unsigned)((ny + 7) / 8), (unsigned)(nz < 65535 ? nz : 65535));
     ccl_union<<<ug, ub, 0, st>>>(d_mask, d_par, (int)nx, (int)ny, (int)nz, bg);
+    ccl_starts<<<(unsigned)((rows + 7) / 8), 256, 0, st>>>(d_mask, d_par, (int)nx, rows, bg, d_cnt, d_bits);
+    ccl_scan_chunks<<<1, 1024, 0, st>>>(d_cnt, nchunks);
+    ccl_rank<<<nchunks, kRankThreads, 0, st>>>(d_bits, (n + 31) / 32, d_cnt, d_labels);
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const unsigned flat_blocks = (unsigned)sms * 8u;
-    ccl_flatten<<<flat_blocks, 256, 0, st>>>(d_par, n);
-    const uint32_t nchunks = (n + kChunk - 1) / kChunk;
-    ccl_count<<<nchunks, kRankThreads, 0, st>>>(d_par, n, d_cnt);
-    ccl_scan_chunks<<<1, 1024, 0, st>>>(d_cnt, nchunks);
-    ccl_rank<<<nchunks, kRankThreads, 0, st>>>(d_par, n, d_cnt, d_labels);
-    ccl_relabel<<<flat_blocks, 256, 0, st>>>(d_par, n, d_labels);
+    ccl_relabel<<<(unsigned)sms * 8u, 256, 0, st>>>(d_par, n, d_labels);
     CK(cudaGetLastError());
     uint32_t roots = 0;
     CK(cudaMemcpyAsync(&roots, d_cnt + nchunks, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -330,10 +398,12 @@ int label_common(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz, uint
                  uint32_t *num_labels, uint8_t *boundary, uint64_t boundary_cap, cudaStream_t st)
 {
     const uint32_t n = (uint32_t)(nx * ny * nz);
-    const uint32_t nchunks = (n + kChunk - 1) / kChunk;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    ft_retain_pool_memory(dev);
     uint32_t *d_par = nullptr, *d_cnt = nullptr;
     CK(cudaMallocAsync((void **)&d_par, (size_t)n * 4, st));
-    cudaError_t e = cudaMallocAsync((void **)&d_cnt, ((size_t)nchunks + 1) * 4, st);
+    cudaError_t e = cudaMallocAsync((void **)&d_cnt, scratch_words(n) * 4, st);
     if (e != cudaSuccess) {
         cudaFreeAsync(d_par, st);
         return ft_fail(FAST_NOMEM, "labelling scratch: %s", cudaGetErrorString(e));

@@ -4,3 +4,9 @@
 
 int ft_fail(int status, const char *fmt, ...);
 void ft_clear_error();
+
+// Keep memory freed into the device's default stream-ordered pool for the
+// next call of the library (its solves, labellings and area passes
+// allocate their scratch from that pool), instead of returning it to the
+// driver at every synchronisation.  Applied once per device.
+void ft_retain_pool_memory(int device);

@@ -58,6 +58,19 @@ int ft_fail(int status, const char *fmt, ...)
 
 void ft_clear_error() { g_last_error.clear(); }
 
+void ft_retain_pool_memory(int device)
+{
+    static std::once_flag once[64];
+    if (device < 0 || device >= 64) return;
+    std::call_once(once[device], [device] {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t thr = std::numeric_limits<uint64_t>::max();
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    });
+}
+
 #define CU(call)                                                                                   \
     do {                                                                                           \
         cudaError_t e_ = (call);                                                                   \
@@ -83,12 +96,7 @@ int Engine::init(int dev)
     if (ce == cudaSuccess) ce = configure_f32();
     if (ce == cudaSuccess) ce = configure_misc();
     if (ce != cudaSuccess) return fail(FAST_CUDA_ERROR, "kernel configuration: %s", cudaGetErrorString(ce));
-    // Keep freed pool memory for reuse by the next solve.
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-        uint64_t thr = std::numeric_limits<uint64_t>::max();
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-    }
+    ft_retain_pool_memory(dev);
     return FAST_OK;
 }
 
