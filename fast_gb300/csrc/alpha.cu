@@ -263,8 +263,12 @@ __device__ __forceinline__ int cube_of(uint32_t cnt, int thr)
 // on every run.
 constexpr int QCAP = 2048;
 
+// The seven-field pass is held to 64 registers (4 blocks per SM, a few
+// hundred bytes of spills): its memory waits want the warps more than the
+// registers (1024^3 tensor pass 62.9 ms at 128 registers and 2 blocks, 61.3
+// at 3 blocks, 58.7 at 4).
 template <bool LABELS>
-__global__ void __launch_bounds__(NT) alpha_kernel(AlphaArgs A)
+__global__ void __launch_bounds__(NT, LABELS ? 4 : 3) alpha_kernel(AlphaArgs A)
 {
     __shared__ uint32_t s_w[3][PH * PW];
     __shared__ McTable s_tab;
