@@ -263,12 +263,13 @@ __device__ __forceinline__ int cube_of(uint32_t cnt, int thr)
 // on every run.
 constexpr int QCAP = 2048;
 
-// The seven-field pass is held to 64 registers (4 blocks per SM, a few
-// hundred bytes of spills): its memory waits want the warps more than the
-// registers (1024^3 tensor pass 62.9 ms at 128 registers and 2 blocks, 61.3
-// at 3 blocks, 58.7 at 4).
+// Both passes are held to 64 registers (4 blocks per SM; the seven-field
+// one spills a few hundred bytes): their memory waits want the warps more
+// than the registers (1024^3: seven fields 62.9 ms at 128 registers and 2
+// blocks, 61.3 at 3, 58.7 at 4; one field 16.1 ms at 75 registers and 3
+// blocks, 14.7 at 4, 15.4 at 5).
 template <bool LABELS>
-__global__ void __launch_bounds__(NT, LABELS ? 4 : 3) alpha_kernel(AlphaArgs A)
+__global__ void __launch_bounds__(NT, 4) alpha_kernel(AlphaArgs A)
 {
     __shared__ uint32_t s_w[3][PH * PW];
     __shared__ McTable s_tab;
