@@ -88,3 +88,18 @@ def test_many_components_boundary_retry(gpu, oracle):
     assert c.num_labels == (m == 0).sum() + 1 > (1 << 20)
     ref_labels, ref_n = oracle.ccl_label(m)
     np.testing.assert_array_equal(c.labels, ref_labels)
+
+
+@pytest.mark.parametrize("shape,frac", [((96, 80, 150), 0.35), ((64, 64, 64), 0.2)])
+def test_dominant_component_repeatable(gpu, oracle, shape, frac):
+    """One component spanning most of the pore space: every join and run
+    start walks to the same root, which is where the concurrent union-find
+    races.  Several calls must give the same labels, equal to the oracle's."""
+    m = volumes.spheres(shape, seed=21, r_min=3.0, r_max=6.0, solid_fraction=frac)
+    ref_labels, ref_n = oracle.ccl_label(m)
+    sizes = np.bincount(ref_labels.ravel())[1:]
+    assert sizes.max() > 0.9 * sizes.sum()  # the case is the dominant-component one
+    for _ in range(4):
+        got = ccl.get_volume_ccl(m)
+        assert got.num_labels == ref_n
+        np.testing.assert_array_equal(got.labels, ref_labels)
