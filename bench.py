@@ -765,7 +765,8 @@ def run_alpha(args):
 
 def run_ncu_case(args):
     """A short, fixed run of the workload's kernels for profiler captures:
-    the bench volume (the 64^3 plain drop-in volume with --workload c1),
+    the bench volume (the 64^3 plain drop-in volume with --workload c1, the
+    large-volume spheres at --c5-edge with --workload c5),
     one direction (x), BiCGSTAB (or CG with --ncu-solver cg) in MIXED (FP64
     for c1, or --ncu-precision) stopped after --ncu-iters iterations.
     Prints the iteration count; times nothing."""
@@ -776,6 +777,11 @@ def run_ncu_case(args):
         name = "c1_spheres64"
         mask = volumes.spheres((64, 64, 64), seed=0, r_min=5.0, solid_fraction=0.60)
         prec = args.ncu_precision or "f64"
+    elif args.workload == "c5":
+        n = args.c5_edge
+        name = f"c5_spheres{n}"
+        mask = volumes.spheres((n, n, n), seed=7, r_min=10.0, solid_fraction=0.65)
+        prec = args.ncu_precision or "mixed"
     else:
         name = WORKLOAD["name"]
         mask = make_volume()
