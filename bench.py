@@ -388,6 +388,10 @@ C_RESULT_BYTES = 40  # sizeof(fast_tau_result)
 # (profiles/), scaled by 3 to the three right-hand sides a bench launch
 # processes (traffic grows with the voxels).
 NCU_TRAFFIC = {"bi1": 3 * 669.7e6, "bi2": 3 * 275.3e6}
+# DRAM bytes per voxel-iteration of the two PCG sweeps at the large-volume
+# slab depth (ncu dram__bytes_read.sum + dram__bytes_write.sum of OpCG1 and
+# OpCG2 on the 512^3 spheres at 256 planes per block: 13.02 + 21.11).
+C5_DRAM_BYTES_PER_VOXEL_ITER = 34.13
 
 
 # ---------------------------------------------------------------------------
@@ -663,6 +667,8 @@ def run_c5(args):
     N = n ** 3
     iter_ms = sum(prof.get(k, {"ms": 0})["ms"] for k in ("cg1", "cg2", "replace"))
     gbs = 25.0 * N * res.iterations / (iter_ms / 1e3) / 1e9
+    sweep_ms = sum(prof.get(k, {"ms": 0})["ms"] for k in ("cg1", "cg2"))
+    dram_gbs = C5_DRAM_BYTES_PER_VOXEL_ITER * N * res.iterations / (sweep_ms / 1e3) / 1e9
     peak, kind = load_peaks()
     ref = None
     if not args.c5_no_reference:
@@ -675,6 +681,9 @@ def run_c5(args):
                  tau=res.tau, iterations=res.iterations, status=int(res.status),
                  stencil_iteration={"gbs_at_25B": gbs, "peak": peak, "peak_kind": kind, "frac": gbs / peak,
                                     "frac_of_8000": gbs / 8000.0,
+                                    "dram_gbs": dram_gbs, "dram_frac": dram_gbs / peak,
+                                    "dram_frac_of_8000": dram_gbs / 8000.0,
+                                    "dram_bytes_per_voxel_iter": C5_DRAM_BYTES_PER_VOXEL_ITER,
                                     "kernel_ms": {k: round(v["ms"], 2) for k, v in prof.items()}},
                  ccl={"seconds": t_ccl, "num_labels": c.num_labels, "canonical_order": canonical,
                       "pore_voxels": pores, "x_spanning_components": int(spanning[1:].sum()),
