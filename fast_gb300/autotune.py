@@ -72,7 +72,8 @@ def set_slab_table(precision: Precision, solver: DiffusionSolverType, depths: Op
 def rule_depth(shape, nrhs: int, precision: Precision, solver: DiffusionSolverType) -> int:
     """The depth of the block-count rule (the full depth, halved while the
     launch has fewer than 608 blocks): the library's choice with an empty
-    table."""
+    table.  Leaves the built-in table installed for this precision and
+    solver (a table installed earlier in the process is replaced)."""
     lib = _native.lib()
     zeros = (C.c_int32 * NUM_CLASSES)()
     old = os.environ.pop("FAST_TAU_ZC", None)
