@@ -140,10 +140,18 @@ __global__ void ccl_union(const uint8_t *__restrict__ m, uint32_t *par, int nx, 
     const uint32_t sy = (uint32_t)nx, sz = (uint32_t)nx * (uint32_t)ny;
     for (int z = blockIdx.z; z < nz; z += gridDim.z) {
         const uint32_t i = (uint32_t)x + sy * (uint32_t)y + sz * (uint32_t)z;
-        if (m[i] == bg) continue;
-        const bool left = x > 0 && m[i - 1] != bg;
-        if (y > 0 && m[i - sy] != bg && !(left && m[i - 1 - sy] != bg)) unite(par, i, i - sy);
-        if (z > 0 && m[i - sz] != bg && !(left && m[i - 1 - sz] != bg)) unite(par, i, i - sz);
+        // The six mask bytes are loaded together (one round trip), not one
+        // behind the other's branch.
+        const uint8_t c = m[i];
+        const uint8_t l = x > 0 ? m[i - 1] : bg;
+        const uint8_t u = y > 0 ? m[i - sy] : bg;
+        const uint8_t ul = (x > 0 && y > 0) ? m[i - 1 - sy] : bg;
+        const uint8_t b = z > 0 ? m[i - sz] : bg;
+        const uint8_t bl = (x > 0 && z > 0) ? m[i - 1 - sz] : bg;
+        if (c == bg) continue;
+        const bool left = l != bg;
+        if (u != bg && !(left && ul != bg)) unite(par, i, i - sy);
+        if (b != bg && !(left && bl != bg)) unite(par, i, i - sz);
     }
 }
 
