@@ -129,3 +129,30 @@ def test_measured_table_is_used_by_the_solver(gpu, clean_table, monkeypatch):
     forced = ft.get_tortuosity(m, p, ft.DSOLVER_CG)
     assert tuned == forced  # the same depth, the same summation order
     assert tuned > 1.0
+
+
+def test_cli_merges_timing_files_and_writes_table(tmp_path, clean_table):
+    """--from-json a,b: a case in b replaces the same case in a; the written
+    header holds the resulting depths."""
+    import json
+
+    def row(edge, prec, solver, times):
+        return {"edge": edge, "nrhs": 1, "precision": prec, "solver": solver,
+                "class": at.slab_depth((edge,) * 3, 1, ft.Precision[prec], ft.DiffusionSolverType(solver))[1],
+                "voxels": edge ** 3, "span": 16, "s_per_iter": times}
+
+    a = tmp_path / "a.json"
+    b = tmp_path / "b.json"
+    a.write_text(json.dumps({"device": "test GPU", "rows": [
+        row(128, "MIXED", 1, {"8": 1.0e-3, "16": 2.0e-3}),
+        row(64, "F64", 0, {"2": 2.0e-3, "4": 1.0e-3})]}))
+    b.write_text(json.dumps({"rows": [row(128, "MIXED", 1, {"8": 3.0e-3, "16": 1.0e-3})]}))
+    out = tmp_path / "table.inc"
+    assert at.main(["--from-json", f"{a},{b}", "--write", str(out)]) == 0
+    text = out.read_text()
+    assert "Measured on test GPU" in text
+    rows = [[int(v) for v in r.split(",")] for r in re.findall(r"\{([0-9, ]+)\},\s*// DSOLVER_", text)]
+    mixed_cg, f64_bicg = rows[5], rows[0]
+    assert mixed_cg[12] == 16  # b's timing of the 128^3 case replaced a's
+    assert f64_bicg[9] == 4
+    assert rows[2] == [0] * 32  # no F32 BiCGSTAB rows: no entries
