@@ -1,9 +1,10 @@
 // Pore count that allocates nothing.
 //
-// Some callers cannot allocate device memory: code running while a stream is
-// being captured into a CUDA graph (cudaMalloc is not allowed there), or a
-// host application whose device memory is entirely owned by its own
-// allocator.  fast_porosity_device_noalloc serves them: the caller passes the
+// Some callers cannot allocate device memory: a host application whose own
+// allocator has reserved all of the GPU's memory (a caching allocator that
+// owns the device, so a cudaMalloc from a library fails or fragments its
+// pool), or a plug-in host that forbids its plug-ins to allocate device
+// memory.  fast_porosity_device_noalloc serves them: the caller passes the
 // device-resident mask and a host output, and the reduction's scratch (one
 // partial count per block, an arrival counter and the total) lives in the
 // file-scope array below instead of memory allocated per call.
@@ -13,6 +14,12 @@
 // call shares it: calls whose work overlaps on the GPU (different streams or
 // threads, no ordering between them) race on it and must be serialised by the
 // caller.
+//
+// The first call on a device looks up the array's device address (with that
+// device current) and keeps it for the life of the process; make one complete
+// call on each device before any stream capture, which also loads the kernel
+// under lazy module loading.  The kept address is not valid after a
+// cudaDeviceReset of that device.
 #include <cuda_runtime.h>
 
 #include <cstdint>

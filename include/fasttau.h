@@ -246,16 +246,19 @@ FAST_API int fast_tau_set_slab_table(int32_t precision, int32_t solver, const in
                                      int32_t nclass);
 
 /* Pore count of a DEVICE-resident mask that allocates nothing, for callers
- * that cannot allocate device memory: code running while a stream is being
- * captured into a CUDA graph, or an application whose device memory is owned
- * by its own allocator.  No counterpart in the reference.  The reduction's
- * scratch is a 256 KiB static device array inside the library, held by every
- * GPU that loads the library until exit; volumes above 2,145,386,496 voxels
- * (32736 blocks x 65536 voxels) are rejected with FAST_BAD_ARG.  The first
- * call on a device looks up the array's device address: make it before any
- * stream capture.  All calls share the array, so calls that overlap on the
- * GPU race.  stream: a cudaStream_t as void*, NULL = the legacy default
- * stream; the call synchronises it.  porosity is nullable. */
+ * that cannot allocate device memory: an application whose own allocator has
+ * reserved all of the GPU's memory, or a plug-in host that forbids its
+ * plug-ins to allocate device memory.  No counterpart in the reference.  The
+ * reduction's scratch is a 256 KiB static device array inside the library,
+ * held by every GPU that loads the library until exit; volumes above
+ * 2,145,386,496 voxels (32736 blocks x 65536 voxels) are rejected with
+ * FAST_BAD_ARG.  The first call on a device looks up the array's device
+ * address and loads the kernel: make one complete call on each device before
+ * any stream capture.  The address is kept for the life of the process and
+ * is not valid after a cudaDeviceReset.  All calls share the array, so calls
+ * that overlap on the GPU race.  stream: a cudaStream_t as void*, NULL = the
+ * legacy default stream; the call copies the count into host memory and
+ * synchronises that stream before it returns.  porosity is nullable. */
 FAST_API int fast_porosity_device_noalloc(const uint8_t *d_mask, int64_t nx, int64_t ny, int64_t nz,
                                           uint64_t *pore_count, double *porosity, void *stream);
 

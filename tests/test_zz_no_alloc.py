@@ -1,6 +1,7 @@
 """The allocation-free pore count, for callers that cannot allocate device
-memory (stream capture in progress, or a foreign allocator owning the GPU's
-memory): called through the C ABI on a device mask, it must give the same
+memory (an application whose own allocator has reserved all of the GPU's
+memory, or a plug-in host that forbids device allocation): called through the
+C ABI on a device mask, it must give the same
 count as the allocating fast_porosity, on two calls in a row that share its
 static scratch.  Counts are integers, so the comparison is exact.
 
@@ -40,6 +41,29 @@ def test_noalloc_pore_count_matches_fast_porosity(gpu):
         assert st == 0, L.fast_last_error()
         ref_cnt, ref_phi = _allocating_count(L, m)
         assert cnt.value == ref_cnt == int((m == 0).sum())
+        assert phi.value == ref_phi
+
+
+def test_noalloc_on_a_side_stream_with_many_blocks(gpu):
+    """About 100 M voxels (1526 blocks of the last-block-done reduction) on a
+    non-default stream, twice in a row, against the allocating count."""
+    torch = pytest.importorskip("torch")
+    L = gpu
+    rng = np.random.default_rng(33)
+    m = ((rng.random((400, 500, 500), dtype=np.float32) < 0.37) * 255).astype(np.uint8)
+    nz, ny, nx = m.shape
+    ref_cnt, ref_phi = _allocating_count(L, m)
+    assert ref_cnt == int((m == 0).sum())
+    side = torch.cuda.Stream()
+    d = torch.from_numpy(m).cuda()
+    side.wait_stream(torch.cuda.current_stream())
+    for _ in range(2):
+        cnt = C.c_uint64(0)
+        phi = C.c_double(0)
+        st = L.fast_porosity_device_noalloc(C.c_void_p(d.data_ptr()), nx, ny, nz, C.byref(cnt), C.byref(phi),
+                                            C.c_void_p(side.cuda_stream))
+        assert st == 0, L.fast_last_error()
+        assert cnt.value == ref_cnt
         assert phi.value == ref_phi
 
 
