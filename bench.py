@@ -147,6 +147,24 @@ def dist_init():
     return ws, rank, local
 
 
+def spawn_replicas(n: int, argv) -> int:
+    """`bench.py --gpus N` started without a launcher: start N copies of this
+    script, one per GPU (RANK = LOCAL_RANK = 0..N-1, gloo rendezvous on
+    127.0.0.1), as torchrun would, and return the worst exit code."""
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__)] + list(argv), env=env))
+    codes = [p.wait() for p in procs]
+    return next((c for c in codes if c != 0), 0)
+
+
 def barrier(ws):
     if ws > 1:
         import torch.distributed as dist
@@ -163,66 +181,90 @@ def max_over_ranks(v: float, ws: int) -> float:
     return float(t.item())
 
 
-def make_volume():
-    from fast_gb300 import volumes
+def make_volume(use_oracle_generator: bool = False):
+    """The benchmark volume.  The CPU arms take it from the oracle's build of
+    the generator (the same source file as libfasttau.so's fast_gen_*), so a
+    process that times only the CPU path never loads the CUDA library; its
+    SHA-256 is checked against the golden record."""
     w = WORKLOAD
+    if use_oracle_generator:
+        from oracle import oracle as O
+        m = O.gen_ellipsoids(w["shape"], w["seed"], w["semi_major"], w["aspect"], w["solid_fraction"])
+        g = load_golden()
+        if g:
+            import hashlib
+            if hashlib.sha256(m.tobytes()).hexdigest() != g["sha256"]:
+                raise RuntimeError("the generated benchmark volume does not match its golden SHA-256")
+        return m
+    from fast_gb300 import volumes
     return volumes.ellipsoids(w["shape"], w["seed"], w["semi_major"], w["aspect"], w["solid_fraction"])
 
 
-def full_cpu_iters(g) -> int:
-    """Iterations of the reference's --cpu FP64 BiCGSTAB (Eigen) at the
-    workload's tolerance on direction x (golden fixture; oracle-computed)."""
-    if g:
-        rec = g["dirs"]["0"]
-        for k in ("iters_bicgstab_eigen_1e-7", "iters_bicgstab_1e-7", "iters_bicgstab_1e-6"):
-            if k in rec:
-                return int(rec[k])
-    return 1000
+def workload_config():
+    """The workload both arms measure (the same dict in both JSON lines)."""
+    w = WORKLOAD
+    return {"workload": w["name"], "volume": "256^3 ellipsoids seed 1 a=12 aspect 0.35 solid 0.55",
+            "solver": "BiCGSTAB, Jacobi", "dirs": "x,y,z", "tol": w["tol"],
+            "l2": "working set > 129 MB L2 (GPU ~2.4 GB per step); no flush"}
 
 
-def cpu_sample(mask, dir_: int, full_iters: int, threads: int):
-    """Times the CPU oracle (stored system + BiCGSTAB, FP64) on this volume:
-    two bounded runs (5 and 25 iterations) give the setup and per-iteration
-    cost; a full solve is extrapolated to `full_iters` iterations."""
+def cpu_solve(mask, dir_: int):
+    """One full solve on the host cores: the oracle's FP64 BiCGSTAB in the
+    Eigen recurrence (the reference's --cpu path: stored 7-coefficient system,
+    diagonal preconditioner) at the workload's tolerance, timed like the
+    reference's tauTime (assembly + solve + tau, TauModule.h:87-99).
+    Returns (seconds, result)."""
     from oracle import oracle as O
     O.build()
-    t = {}
-    for n in (5, 25):
-        t0 = time.perf_counter()
-        O.get_tortuosity(mask, dir=dir_, solver=O.BICGSTAB, tol=WORKLOAD["tol"], max_iter=n, variant=O.EIGEN)
-        t[n] = time.perf_counter() - t0
-    per_iter = max((t[25] - t[5]) / 20.0, 1e-9)
-    setup = max(t[5] - 5 * per_iter, 0.0)
-    est = setup + full_iters * per_iter
-    return est, setup, per_iter, t[5] + t[25]
+    t0 = time.perf_counter()
+    r = O.get_tortuosity(mask, dir=dir_, solver=O.BICGSTAB, tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"],
+                         variant=O.EIGEN)
+    return time.perf_counter() - t0, r
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
 
 
 def run_reference(args, ws, rank):
-    """--impl reference: the CPU restatement of the reference's path."""
+    """--impl reference: the reference's CPU path (restated by the oracle;
+    the reference itself cannot be built here) on the same workload, every
+    host thread.  Each timed step is one complete solve, the direction
+    cycling x, y, z from step to step; warm-up steps run the assembly and
+    five iterations (they fault in memory and start the thread pool).  Only
+    rank 0 works and prints; other ranks return at once."""
     if rank != 0:
         return
-    mask = make_volume()
-    g = load_golden()
-    full = full_cpu_iters(g)
-    threads = os.cpu_count() or 1
-    per_step = []
-    for i in range(args.warmup + args.steps):
-        est, setup, per_iter, wall = cpu_sample(mask, 0, full, threads)
-        if i >= args.warmup:
-            per_step.append(est)
-    t = statistics.mean(per_step)
-    value = 1.0 / t
+    from oracle import oracle as O
+    mask = make_volume(use_oracle_generator=True)
+    dirs = list(WORKLOAD["dirs"])
+    for _ in range(args.warmup):
+        O.get_tortuosity(mask, dir=0, solver=O.BICGSTAB, tol=WORKLOAD["tol"], max_iter=5, variant=O.EIGEN)
+    secs, per_dir = [], {}
+    for i in range(args.steps):
+        d = dirs[i % len(dirs)]
+        t, r = cpu_solve(mask, d)
+        secs.append(t)
+        per_dir.setdefault(str(d), []).append({"seconds": t, "iterations": r["iters"], "status": r["status"],
+                                               "tau": r["tau"]})
+    total = sum(secs)
+    value = args.steps / total
+    threads = cpu_threads()
     line = {
-        "metric": "tau solves/s", "value": value, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD["name"], "volume": "256^3 ellipsoids seed 1 a=12 aspect 0.35 solid 0.55",
-                   "solver": "BiCGSTAB (Eigen recurrence, Jacobi)", "dirs": "x (one solve per step)",
-                   "tol": WORKLOAD["tol"]},
+        "metric": "tau solves/s", "value": value, "unit": "solves/s", "impl": "reference", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded ellipsoid packing stand-in)", "config": workload_config(),
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": f"oracle FP64 BiCGSTAB on the 256^3 volume, direction x: assembly + 5 and + 25 "
-                                   f"iterations timed, extrapolated to the {full} iterations of a full "
-                                   f"tol-{WORKLOAD['tol']:g} solve"},
+                         "sample": f"{args.steps} complete FP64 BiCGSTAB solves (Eigen recurrence, Jacobi, tol "
+                                   f"{WORKLOAD['tol']:g}) of the 256^3 volume, one direction per step cycling "
+                                   f"x, y, z; assembly + solve + tau timed; no extrapolation"},
+        "per_direction": {k: {"mean_seconds": statistics.mean(e["seconds"] for e in v),
+                              "iterations": v[0]["iterations"], "tau": v[0]["tau"],
+                              "all_converged": all(e["status"] == 0 for e in v)} for k, v in per_dir.items()},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -341,23 +383,20 @@ def run_ours(args, ws, rank, local):
 
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        full = full_cpu_iters(g)
-        threads = os.cpu_count() or 1
-        est, setup, per_iter, wall = cpu_sample(mask, 0, full, threads)
-        cpu = {"value": 1.0 / est, "unit": "solves/s", "cores": threads, "kind": "port",
-               "sample": f"oracle FP64 BiCGSTAB (Eigen recurrence, the reference --cpu path) on this volume, direction x: setup + 5 and "
-                         f"+ 25 iterations timed ({wall:.1f} s), extrapolated to the {full} iterations of a full "
-                         f"tol-{w['tol']:g} solve: {setup:.2f} s + {per_iter * 1e3:.1f} ms/iter"}
+        secs, r = cpu_solve(mask, 0)
+        cpu = {"value": 1.0 / secs, "unit": "solves/s", "cores": cpu_threads(), "kind": "port",
+               "sample": f"one complete solve of this volume in x: the oracle's FP64 BiCGSTAB (Eigen recurrence, "
+                         f"the reference --cpu path; Jacobi, tol {w['tol']:g}), assembly + solve + tau, "
+                         f"{r['iters']} iterations in {secs:.1f} s; no extrapolation",
+               "tau": r["tau"], "iterations": r["iters"]}
 
     line = {
         "metric": "tau solves/s", "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded ellipsoid packing stand-in)",
-        "config": {"workload": w["name"], "volume": "256^3 ellipsoids seed 1 a=12 aspect 0.35 solid 0.55",
-                   "solver": "BiCGSTAB, Jacobi", "dirs": "x,y,z as 3 RHS",
-                   "precision": "FP32 iterations + FP64 residual replacement",
-                   "tol": w["tol"], "parallelism": f"replicas x{ws}",
-                   "l2": "working set ~2.4 GB per step > 129 MB L2; no flush"},
+        "config": workload_config(),
+        "precision": "FP32 iterations + FP64 residual replacement", "parallelism": f"replicas x{ws}",
+        "rhs": "x, y, z as 3 right-hand sides of one launch sharing the phase field",
         "voxel_iters_per_s": N * (sum(iters) / len(iters)) * ws / (ms_max / 1e3 / args.steps),
         "iterations_per_step": sum(iters) / len(iters),
         "all_converged": ok,
@@ -825,7 +864,22 @@ def main():
                     help="c4: requests timed on the plain solver (0: all of them)")
     ap.add_argument("--c5-edge", type=int, default=1024)
     ap.add_argument("--c5-no-reference", action="store_true")
+    ap.add_argument("--replica-check", action="store_true",
+                    help="start the ranks, meet in a barrier and a max over ranks, print them and exit")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(spawn_replicas(args.gpus, sys.argv[1:]))
+    if args.replica_check:
+        ws, rank, local = dist_init()
+        barrier(ws)
+        m = max_over_ranks(1.5 + rank, ws)
+        if rank == 0:
+            print(json.dumps({"replica_check": True, "world_size": ws, "max_over_ranks": m}), flush=True)
+        barrier(ws)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
     if args.ncu_case:
         from fast_gb300 import build
         build.build()

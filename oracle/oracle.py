@@ -32,12 +32,18 @@ D0_F32 = float(np.float32(1.0))
 D1_F32 = float(np.float32(0.001))
 
 
+_GEN_SO = os.path.join(_HERE, "_build", "libvolgen.so")
+_GEN_SRC = os.path.join(_HERE, os.pardir, "fast_gb300", "csrc", "gen.cpp")
+_gen = None
+
+
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (gcc, OpenMP)."""
+    """Compile the oracle and the volume generator with the Makefile (gcc,
+    OpenMP; g++ for the generator)."""
     srcs = [os.path.join(_HERE, f) for f in ("tau_oracle.c", "tau_oracle_impl.h", "ccl_oracle.c", "alpha_oracle.c",
-                                             "Makefile")]
-    if not force and os.path.exists(_SO):
-        so_m = os.path.getmtime(_SO)
+                                             "Makefile")] + [_GEN_SRC]
+    if not force and os.path.exists(_SO) and os.path.exists(_GEN_SO):
+        so_m = min(os.path.getmtime(_SO), os.path.getmtime(_GEN_SO))
         if all(os.path.getmtime(s) <= so_m for s in srcs):
             return _SO
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -77,6 +83,38 @@ def lib():
             L.oracle_mc_ntri.restype = i32
             _lib = L
     return _lib
+
+
+def _volgen():
+    """libvolgen.so: the seeded generator without the CUDA library."""
+    global _gen
+    with _lock:
+        if _gen is None:
+            build()
+            G = C.CDLL(_GEN_SO)
+            G.fast_gen_spheres.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_double,
+                                           C.c_double, C.c_double]
+            G.fast_gen_ellipsoids.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_double,
+                                              C.c_double, C.c_double]
+            G.fast_gen_spheres.restype = G.fast_gen_ellipsoids.restype = C.c_int
+            _gen = G
+    return _gen
+
+
+def gen_spheres(shape, seed, r_min, r_max, solid_fraction):
+    """The same bytes as fast_gb300.volumes.spheres (same source file)."""
+    nz, ny, nx = shape
+    out = np.empty((nz, ny, nx), dtype=np.uint8)
+    assert _volgen().fast_gen_spheres(_ptr(out), nx, ny, nz, seed, r_min, r_max, solid_fraction) == OK
+    return out
+
+
+def gen_ellipsoids(shape, seed, semi_major, aspect, solid_fraction):
+    """The same bytes as fast_gb300.volumes.ellipsoids (same source file)."""
+    nz, ny, nx = shape
+    out = np.empty((nz, ny, nx), dtype=np.uint8)
+    assert _volgen().fast_gen_ellipsoids(_ptr(out), nx, ny, nz, seed, semi_major, aspect, solid_fraction) == OK
+    return out
 
 
 def _ptr(a: np.ndarray):

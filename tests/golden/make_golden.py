@@ -17,7 +17,22 @@ the same numbers:
                     for the benchmark volumes (64^3 spheres; 256^3 ellipsoids,
                     three directions).
 
-Usage:  python tests/golden/make_golden.py [small|workloads|bicgstab1e-7|all]
+  large (CPU, a minute): the 1024^3 large-volume spheres (seed 7, r = 10,
+                    solid 0.65): the volume's SHA-256 and pore count, and the
+                    oracle's connected-component labels of the pore phase
+                    (label count, SHA-256 of the uint32 label array, SHA-256 of
+                    the 7 x K face table).
+  large_tau OUT     (GPU, about a minute): FP64 tau of that volume in x at tol
+                    1e-10.  The oracle's stored-coefficient system of a 1024^3
+                    volume needs 77 GB of host memory, so the GPU's FP64
+                    Jacobi-PCG, the reference-semantics path that the parity
+                    tests check against the oracle up to 256^3, stands in; the
+                    record goes to OUT (JSON) and `merge OUT` adds it to
+                    workloads.json.
+
+Usage:  python tests/golden/make_golden.py [small|workloads|bicgstab1e-7|large|all]
+        python tests/golden/make_golden.py large_tau OUT
+        python tests/golden/make_golden.py merge OUT
 """
 import hashlib
 import json
@@ -188,8 +203,79 @@ def workloads_bicgstab_1e7():
         json.dump(doc, f, indent=1)
 
 
+LARGE = dict(kind="spheres", shape=(1024, 1024, 1024), seed=7, r=10.0, frac=0.65)
+
+
+def large_volume():
+    return volumes.spheres(LARGE["shape"], LARGE["seed"], LARGE["r"], LARGE["r"], LARGE["frac"])
+
+
+def large():
+    """Volume hash, pore count and the oracle's labels of the 1024^3 volume."""
+    path = os.path.join(HERE, "workloads.json")
+    with open(path) as f:
+        doc = json.load(f)
+    m = large_volume()
+    t0 = time.time()
+    labels, n = O.ccl_label(m)
+    table = O.ccl_boundary(labels, n)
+    e = doc["workloads"].setdefault("spheres1024", {})
+    e.update(spec=dict(LARGE, shape=list(LARGE["shape"])), sha256=sha(m), pores=int((m == 0).sum()),
+             ccl={"num_labels": int(n), "labels_sha256": sha(labels), "boundary_sha256": sha(table),
+                  "x_spanning": int((table[0] & table[1])[1:].sum()),
+                  "seconds": time.time() - t0})
+    e.setdefault("dirs", {})
+    print("spheres1024", e["sha256"], e["pores"], e["ccl"], flush=True)
+    with open(path, "w") as f:
+        json.dump(doc, f, indent=1)
+
+
+def large_tau(out):
+    """FP64 tau of the 1024^3 volume in x at tol 1e-10 on the GPU (FP64
+    Jacobi-PCG, reference semantics), written to `out`."""
+    import torch
+    import fast_gb300 as ft
+    m = large_volume()
+    h = sha(m)
+    d = torch.from_numpy(m).cuda()
+    del m
+    p = ft.TortuosityParams(tolerance=1e-10, max_iter=200000, precision=ft.Precision.F64)
+    t0 = time.time()
+    r = ft.solve_directions_device(d.data_ptr(), LARGE["shape"], [ft.Dir.X_POS], p, ft.DSOLVER_CG)[0]
+    torch.cuda.synchronize()
+    rec = {"sha256": h, "dirs": {"0": {"tau_cg_1e-10": r.tau, "iters_cg_1e-10": int(r.iterations),
+                                        "status_cg_1e-10": int(r.status), "solver_cg_1e-10": "GPU F64 Jacobi-PCG",
+                                        "seconds": time.time() - t0}}}
+    print(json.dumps(rec), flush=True)
+    with open(out, "w") as f:
+        json.dump(rec, f, indent=1)
+
+
+def merge(frag):
+    path = os.path.join(HERE, "workloads.json")
+    with open(path) as f:
+        doc = json.load(f)
+    with open(frag) as f:
+        rec = json.load(f)
+    e = doc["workloads"]["spheres1024"]
+    assert rec["sha256"] == e["sha256"], "the GPU host generated another volume"
+    for d, v in rec["dirs"].items():
+        e["dirs"].setdefault(d, {}).update(v)
+    with open(path, "w") as f:
+        json.dump(doc, f, indent=1)
+
+
 if __name__ == "__main__":
     what = sys.argv[1] if len(sys.argv) > 1 else "all"
+    if what == "large_tau":
+        large_tau(sys.argv[2])
+        sys.exit(0)
+    if what == "merge":
+        merge(sys.argv[2])
+        sys.exit(0)
+    if what == "large":
+        large()
+        sys.exit(0)
     if what in ("small", "all"):
         small_cases()
     if what in ("workloads", "all"):

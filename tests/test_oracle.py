@@ -270,3 +270,18 @@ def test_independent_scipy_assembly(oracle):
         assert rel(got["tau"], ref) < 1e-8, (m.shape, d, got["tau"], ref)
 
     check()
+
+
+def test_oracle_generator_reproduces_benchmark_volume(oracle):
+    """The CPU arms build the benchmark volume without the CUDA library; the
+    oracle's build of the generator must give the golden bytes, and the same
+    bytes as the product library's fast_gen_* on other shapes."""
+    from fast_gb300 import volumes
+    with open(os.path.join(GOLDEN, "workloads.json")) as f:
+        g = json.load(f)["workloads"]["ellipsoids256"]
+    s = g["spec"]
+    m = oracle.gen_ellipsoids(tuple(s["shape"]), s["seed"], s["a"], s["aspect"], s["frac"])
+    assert hashlib.sha256(m.tobytes()).hexdigest() == g["sha256"]
+    a = oracle.gen_spheres((21, 30, 17), 9, 2.0, 5.0, 0.45)
+    b = volumes.spheres((21, 30, 17), seed=9, r_min=2.0, r_max=5.0, solid_fraction=0.45)
+    assert np.array_equal(a, b)

@@ -56,3 +56,16 @@ def test_two_gloo_ranks_barrier_and_max():
     assert [r[0] for r in res] == [0, 1]
     assert all(r[1] == 2 for r in res)
     assert all(r[3] == 2.5 for r in res)     # both ranks see the slowest rank's time
+
+
+def test_bench_starts_its_own_replicas():
+    """`bench.py --gpus 2` without torchrun starts two ranks itself; they meet
+    in the barrier and the max over ranks, and rank 0 alone prints."""
+    import json
+    import subprocess
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--replica-check"],
+                         capture_output=True, text=True, timeout=300, env=env)
+    assert out.returncode == 0, out.stderr
+    lines = [json.loads(ln) for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert lines == [{"replica_check": True, "world_size": 2, "max_over_ranks": 2.5}]
