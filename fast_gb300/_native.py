@@ -55,6 +55,7 @@ class fast_ctx_stats(C.Structure):
 K_COUNT = 16
 KERNEL_NAMES = ["code", "init", "cg1", "cg2", "bi_restart", "bi1", "bi2", "bi3", "replace", "init64", "tau", "cgf"]
 FLAG_PROFILE = 1
+FLAG_REPLACE_FLOAT_FLOAT = 2
 
 
 class fast_tau_stats(C.Structure):

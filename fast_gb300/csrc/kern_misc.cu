@@ -9,18 +9,26 @@ constexpr int kStages = 3;
 // The replacement slot runs at the head of every iteration and is idle in
 // most: its kernels walk the tiles with one resident wave of blocks
 // (sweep_kernel_tiles), sized here from the occupancy of each kernel.
-int g_resident_bi = 0, g_resident_cg = 0;
+// Index: [float-float][BiCGSTAB].
+int g_resident[2][2] = {};
 
-void launch_replace(bool bicg, const Launch &L, cudaStream_t st)
+template <class Op>
+static void launch_tiles(const Launch &L, cudaStream_t st, int64_t resident)
 {
-    const int64_t resident = bicg ? g_resident_bi : g_resident_cg;
     const unsigned grid = (unsigned)(L.nblocks < resident ? L.nblocks : resident);
-    if (bicg)
-        sweep_kernel_tiles<OpReplaceBi2, kStages>
-            <<<grid, NTHREADS, sweep_dyn_smem<OpReplaceBi2, kStages>(), st>>>(L);
-    else
-        sweep_kernel_tiles<OpReplace<false>, kStages>
-            <<<grid, NTHREADS, sweep_dyn_smem<OpReplace<false>, kStages>(), st>>>(L);
+    sweep_kernel_tiles<Op, kStages><<<grid, NTHREADS, sweep_dyn_smem<Op, kStages>(), st>>>(L);
+}
+
+void launch_replace(bool bicg, bool ff, const Launch &L, cudaStream_t st)
+{
+    const int64_t resident = g_resident[ff][bicg];
+    if (ff) {
+        if (bicg) launch_tiles<OpReplaceBi2<FF>>(L, st, resident);
+        else launch_tiles<OpReplace<false, FF>>(L, st, resident);
+    } else {
+        if (bicg) launch_tiles<OpReplaceBi2<double>>(L, st, resident);
+        else launch_tiles<OpReplace<false, double>>(L, st, resident);
+    }
 }
 
 template <class Op>
@@ -40,9 +48,13 @@ static cudaError_t configure_tiles(int &resident)
 
 cudaError_t configure_misc()
 {
-    cudaError_t a = configure_tiles<OpReplaceBi2>(g_resident_bi);
-    cudaError_t b = configure_tiles<OpReplace<false>>(g_resident_cg);
-    return a != cudaSuccess ? a : b;
+    cudaError_t e[4] = {configure_tiles<OpReplaceBi2<double>>(g_resident[0][1]),
+                        configure_tiles<OpReplace<false, double>>(g_resident[0][0]),
+                        configure_tiles<OpReplaceBi2<FF>>(g_resident[1][1]),
+                        configure_tiles<OpReplace<false, FF>>(g_resident[1][0])};
+    for (cudaError_t x : e)
+        if (x != cudaSuccess) return x;
+    return cudaSuccess;
 }
 
 void launch_init64(const Launch &L, cudaStream_t st) { init64_kernel<<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L); }
@@ -53,6 +65,7 @@ void launch_tau(int src, const Launch &L, cudaStream_t st)
 {
     if (src == 1) tau_kernel<float><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, 0);
     else if (src == 2) tau_kernel<FF><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, 1);
+    else if (src == 3) tau_kernel<double><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, 1);
     else tau_kernel<double><<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L, 0);
 }
 

@@ -114,9 +114,9 @@ int steps_of(const Ctx &C, int solver, std::vector<Step> &steps)
 {
     const bool mixed = C.cfg.precision == FAST_PREC_MIXED;
     if (solver == FAST_SOLVER_CG) {
-        steps = mixed ? mixed_steps(FAST_SOLVER_CG) : std::vector<Step>{Step::CG1, Step::CG2};
+        steps = mixed ? mixed_steps(FAST_SOLVER_CG, false) : std::vector<Step>{Step::CG1, Step::CG2};
     } else {
-        steps = mixed ? std::vector<Step>{Step::REPLACE_BI, Step::BI_K1, Step::BI_K2}
+        steps = mixed ? mixed_steps(FAST_SOLVER_BICGSTAB, false)
                       : std::vector<Step>{Step::BI_RESTART, Step::BI1, Step::BI2, Step::BI3};
     }
     return FAST_OK;
@@ -163,7 +163,7 @@ int retire(Ctx &C, Scalars *snap, uint64_t seq, fast_ctx_completion *out, int32_
         if (s != FAST_OK) return s;
         const Launch L{C.d_tmp[0], (int32_t)jobs.size(), 0, nb};
         const int prec = C.cfg.precision;
-        launch_tau(prec == FAST_PREC_MIXED ? 2 : (prec == FAST_PREC_F32 ? 1 : 0), L, C.st);
+        launch_tau(prec == FAST_PREC_MIXED ? 3 : (prec == FAST_PREC_F32 ? 1 : 0), L, C.st);
         SV(cudaGetLastError());
     }
     // Every retiring solve's final scalars (flux sums included).

@@ -78,6 +78,8 @@ void dispatch_mixed(Step s, const Launch &L, cudaStream_t st);
 // The per-iteration steps of a MIXED solve (CG: one fused sweep, or the
 // classic two with FAST_TAU_CG_FUSED=0).
 bool cg_fused_enabled();
-std::vector<Step> mixed_steps(int solver);
+// MIXED steps of one iteration: the replacement slot (FP64 iterate, or
+// float-float with `ff`) and the FP32 sweeps.
+std::vector<Step> mixed_steps(int solver, bool ff);
 
 }  // namespace ft

@@ -162,7 +162,9 @@ int kind_of(Step s)
     case Step::BI2: return FAST_K_BI2;
     case Step::BI3: return FAST_K_BI3;
     case Step::REPLACE_CG:
-    case Step::REPLACE_BI: return FAST_K_REPLACE;
+    case Step::REPLACE_BI:
+    case Step::REPLACE_CG_FF:
+    case Step::REPLACE_BI_FF: return FAST_K_REPLACE;
     case Step::BI_K1: return FAST_K_BI1;
     case Step::BI_K2: return FAST_K_BI2;
     case Step::CG_F: return FAST_K_CGF;
@@ -393,18 +395,24 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
 
 void dispatch_f64(Step s, const Launch &L, cudaStream_t st) { launch_pure_f64(s, L, st); }
 void dispatch_f32(Step s, const Launch &L, cudaStream_t st) { launch_pure_f32(s, L, st); }
-std::vector<Step> mixed_steps(int solver)
+std::vector<Step> mixed_steps(int solver, bool ff)
 {
-    if (solver == FAST_SOLVER_CG)
-        return cg_fused_enabled() ? std::vector<Step>{Step::REPLACE_CG, Step::CG_F}
-                                  : std::vector<Step>{Step::REPLACE_CG, Step::CG1, Step::CG2};
-    return {Step::REPLACE_BI, Step::BI_K1, Step::BI_K2};
+    if (solver == FAST_SOLVER_CG) {
+        const Step rep = ff ? Step::REPLACE_CG_FF : Step::REPLACE_CG;
+        return cg_fused_enabled() ? std::vector<Step>{rep, Step::CG_F} : std::vector<Step>{rep, Step::CG1, Step::CG2};
+    }
+    return {ff ? Step::REPLACE_BI_FF : Step::REPLACE_BI, Step::BI_K1, Step::BI_K2};
 }
 
 void dispatch_mixed(Step s, const Launch &L, cudaStream_t st)
 {
-    if (s == Step::REPLACE_CG || s == Step::REPLACE_BI) launch_replace(s == Step::REPLACE_BI, L, st);
-    else launch_mixed_inner(s, L, st);
+    switch (s) {
+    case Step::REPLACE_CG: launch_replace(false, false, L, st); break;
+    case Step::REPLACE_BI: launch_replace(true, false, L, st); break;
+    case Step::REPLACE_CG_FF: launch_replace(false, true, L, st); break;
+    case Step::REPLACE_BI_FF: launch_replace(true, true, L, st); break;
+    default: launch_mixed_inner(s, L, st);
+    }
 }
 
 int status_of(int state)
@@ -627,6 +635,12 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     S.cos2_min = cmin * cmin;
     S.inner_mode = mixed ? 1 : 0;
     S.cg_fused = fused ? 1 : 0;
+    J.x64_ff = (mixed && (P.flags & FAST_FLAG_REPLACE_FLOAT_FLOAT)) ? 1 : 0;
+#if defined(FAST_TAU_TEST_HOOKS) && FAST_TAU_TEST_HOOKS
+    // test builds: FAST_TAU_TEST_WITHHOLD = 1 + direction arms the withheld
+    // tile load of that direction's first sweep
+    S.test_withhold = env_int("FAST_TAU_TEST_WITHHOLD", 0) == dir + 1 ? 1 : 0;
+#endif
     // MIXED BiCGSTAB: no update is pending before the first replacement.
     S.alpha = 0.0;
     S.omega = 0.0;
@@ -644,6 +658,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     t_prof.reset((P.flags & FAST_FLAG_PROFILE) != 0);
     const int prec = P.precision, solver = P.solver;
     const bool mixed = prec == FAST_PREC_MIXED;
+    const bool ff = mixed && (P.flags & FAST_FLAG_REPLACE_FLOAT_FLOAT) != 0;
     const int nj = (int)jobs.size(), nv = (int)vols.size();
     if (nj < 1 || nj > Engine::kMaxJobs || nv < 1 || nv > nj)
         return fail(FAST_BAD_ARG, "1..%d right-hand sides per call", Engine::kMaxJobs);
@@ -739,17 +754,17 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
         // the recursion asked for it.
         launch_counted(FAST_K_INIT64, st, [&] { launch_init64(L, st); });
         std::vector<Step> steps;
-        steps = mixed_steps(solver);
+        steps = mixed_steps(solver, ff);
         status = iterate(E, L, nj, d_sc, steps, dispatch_mixed, P.max_iter);
     }
     if (status == FAST_OK)
-        launch_counted(FAST_K_TAU, st, [&] { launch_tau(mixed ? 2 : (prec == FAST_PREC_F32 ? 1 : 0), L, st); });
+        launch_counted(FAST_K_TAU, st, [&] { launch_tau(mixed ? (ff ? 2 : 3) : (prec == FAST_PREC_F32 ? 1 : 0), L, st); });
     CU(cudaMemcpyAsync(hs, d_sc, sizeof(Scalars) * nj, cudaMemcpyDeviceToHost, st));
     if (conc_out && nj == 1) {
         const void *src = hj[0].x;
         size_t es = vec_t;
         CU(cudaStreamSynchronize(st));
-        if (mixed) {
+        if (mixed && ff) {
             // The iterate is float-float: widen it to FP64 in the other
             // ping-pong buffer (free now), then copy that.
             const int cur = hs[0].x64_cur;
@@ -757,6 +772,9 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
             launch_ff_to_double(hj[0].x64[cur], (double *)hj[0].x64[cur ^ 1], n, st);
             CU(cudaGetLastError());
             src = hj[0].x64[cur ^ 1];
+            es = 8;
+        } else if (mixed) {
+            src = hj[0].x64[hs[0].x64_cur];
             es = 8;
         }
         // de-pad the rows: host layout is x-fastest with pitch nx
@@ -810,8 +828,11 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
         }
         if (R.status != FAST_OK && first_bad == FAST_OK) {
             first_bad = R.status;
-            fail(R.status, "right-hand side %d (direction %d): solver %s after %llu iterations (|r|/|b| = %.3e)", j,
-                 jobs[j].dir, R.status == FAST_DIVERGED ? "diverged" : "did not converge",
+            fail(R.status, "right-hand side %d (direction %d): %s after %llu iterations (|r|/|b| = %.3e)", j,
+                 jobs[j].dir,
+                 R.status == FAST_DIVERGED  ? "solver diverged"
+                 : R.status == FAST_TIMEOUT ? "a bounded device-side wait for tile loads ran out"
+                                            : "solver did not converge",
                  (unsigned long long)R.iterations, R.rel_residual);
         }
         if (P.verbose)

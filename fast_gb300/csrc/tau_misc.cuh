@@ -7,34 +7,71 @@
 namespace ft {
 
 // ===========================================================================
+// Arithmetic of the MIXED iterate x64, by its storage type XT (8 bytes per
+// voxel either way): double (the default: the iterate, the correction update
+// and the true residual b - A x in FP64, the stencil and diagonal exactly as
+// the FP64 solver evaluates them) or FF, a float-float pair (an opt-in: about
+// 48 significant bits from error-free FP32 transformations, for when FP64
+// throughput bounds the replacement).
+// ===========================================================================
+template <typename XT>
+struct XArith;
+
+template <>
+struct XArith<double> {
+    using Tab = Coef<double>;
+    __device__ static double add_f(double x, float e) { return x + (double)e; }
+    __device__ static double stencil(const Faces<double> &F, const Tab &C, const Geo &g, uint32_t code,
+                                     const Pos &ps, double fc, double fxp, double fxm, double fyp, double fym,
+                                     double fzp, double fzm)
+    {
+        return stencil7<double>(F, code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag_of<double, false>(C, g, code, ps));
+    }
+    __device__ static float residual32(double b, double ax) { return (float)(b - ax); }
+    __device__ static float to_float(double v) { return (float)v; }
+};
+
+template <>
+struct XArith<FF> {
+    using Tab = Coef<FF>;
+    __device__ static FF add_f(FF x, float e) { return ff_add_f(x, e); }
+    __device__ static FF stencil(const Faces<FF> &F, const Tab &C, const Geo &, uint32_t code, const Pos &ps,
+                                 FF fc, FF fxp, FF fxm, FF fyp, FF fym, FF fzp, FF fzm)
+    {
+        return stencil7_ff(F, code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag_ff(C, code, ps));
+    }
+    __device__ static float residual32(FF b, FF ax) { return ff_to_float(ff_add(b, ff_neg(ax))); }
+    __device__ static float to_float(FF v) { return ff_to_float(v); }
+};
+
+// ===========================================================================
 // MIXED residual replacement.  The FP32 iterations work on a correction e of
-// an extended-precision iterate x64 (a float-float pair per voxel, about 48
-// significant bits); when one of them asks for it (`replace`), this step
+// an extended-precision iterate x64 (FP64 by default, a float-float pair on
+// request; XArith above); when one of them asks for it (`replace`), this step
 // folds e into x64 (x64' = x64 + e, e is zeroed by the next step-1 kernel),
-// recomputes the residual b - A x64' in float-float arithmetic and hands
+// recomputes the residual b - A x64' in that precision and hands
 // fp32 of it to the recursion in place of the recursive residual, keeping
 // the Krylov vectors (replace = 1) or restarting them from it (replace = 2,
 // also the first step of a solve).  The true residual decides convergence.
-// Float-float instead of FP64: the same role (a residual exact to far below
-// FP32 rounding, here about 1e-14 of |A||x|) with FP32 instructions only.
 // Dots, accumulated in FP32 per thread (they steer the iteration and test
 // convergence; they need no more than FP32 accuracy): |fp32(r64)|^2, |b|^2
 // and, for BiCGSTAB, r0.fp32(r64) (r0 = fp32(r64) itself on a restart), for
 // CG fp32(r64).z.  Streams: x64, e, code (+ r0 for BiCGSTAB).
 // ===========================================================================
-template <bool BICG>
+template <bool BICG, typename XT>
 struct OpReplace {
-    using T = FF;
+    using T = XT;
+    using X = XArith<XT>;
     using R = double;
     using SL = typename std::conditional<BICG, Streams<8, 4, 1, 4>, Streams<8, 4, 1>>::type;
     static constexpr int NV = 3;
     using Shared = Coef<float>;
-    struct Vals { FF x; float e; uint32_t code; float r0; };
+    struct Vals { XT x; float e; uint32_t code; float r0; };
     struct Own { uint32_t code; float r0; };
-    struct Out { FF x; float r; };
+    struct Out { XT x; float r; };
     const CUtensorMap *tmap[SL::N];
     Faces<T> F;
-    FF *x64n;
+    XT *x64n;
     float *r, *r0, *p, *v;
     bool restart;
     Acc<float> a_rr, a_bb, a_d;
@@ -43,14 +80,14 @@ struct OpReplace {
     __device__ static void load_shared(Shared &S, const Job &J, int tid) { load_coef<float>(S, J, tid); }
     __device__ static void load2(const unsigned char *st, const Pt &p_, Vals &a, Vals &b)
     {
-        sv2<FF, SL, 0>(st, p_, a.x, b.x);
+        sv2<XT, SL, 0>(st, p_, a.x, b.x);
         sv2<float, SL, 1>(st, p_, a.e, b.e);
         load_code2<SL, 2>(st, p_, a.code, b.code);
         if constexpr (BICG) sv2<float, SL, 3>(st, p_, a.r0, b.r0);
     }
     __device__ static void load1(const unsigned char *st, const Pt &p_, Vals &a)
     {
-        a.x = sv<FF, SL, 0>(st, p_);
+        a.x = sv<XT, SL, 0>(st, p_);
         a.e = sv<float, SL, 1>(st, p_);
     }
     __device__ void init(const Job &J, Shared &)
@@ -65,29 +102,29 @@ struct OpReplace {
         tmap[1] = &J.tm[TM_X];
         tmap[2] = &J.tm[TM_CODE];
         if constexpr (BICG) tmap[3] = &J.tm[TM_R0];
-        x64n = (FF *)J.x64[cur ^ 1];
+        x64n = (XT *)J.x64[cur ^ 1];
         r = (float *)J.r[par];
         r0 = (float *)J.r0;
         p = (float *)J.p[(int)(sc.iter & 1)];
         v = BICG ? (float *)J.v[par] : nullptr;
         restart = sc.replace == 2;
     }
-    __device__ FF field(const Geo &, const Coef<FF> &, Shared &, const Vals &a, const Pos &) const
+    __device__ XT field(const Geo &, const typename X::Tab &, Shared &, const Vals &a, const Pos &) const
     {
-        return ff_add_f(a.x, a.e);
+        return X::add_f(a.x, a.e);
     }
-    __device__ Own own(const Geo &, const Coef<FF> &, Shared &, const Vals &a, const Pos &, FF &f) const
+    __device__ Own own(const Geo &, const typename X::Tab &, Shared &, const Vals &a, const Pos &, XT &f) const
     {
-        f = ff_add_f(a.x, a.e);
+        f = X::add_f(a.x, a.e);
         return Own{a.code, a.r0};
     }
-    __device__ Out apply(const Geo &g, const Coef<FF> &C, Shared &S, const Own &o, const Pos &ps, FF fc, FF fxp,
-                         FF fxm, FF fyp, FF fym, FF fzp, FF fzm)
+    __device__ Out apply(const Geo &g, const typename X::Tab &C, Shared &S, const Own &o, const Pos &ps, XT fc,
+                         XT fxp, XT fxm, XT fyp, XT fym, XT fzp, XT fzm)
     {
-        const FF ax = stencil7_ff(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag_ff(C, o.code, ps));
-        const FF b = rhs_at<FF>(C, g, o.code, ps.x, ps.y, ps.z);
-        const float r32 = ff_to_float(ff_add(b, ff_neg(ax)));
-        const float b32 = ff_to_float(b);
+        const XT ax = X::stencil(F, C, g, o.code, ps, fc, fxp, fxm, fyp, fym, fzp, fzm);
+        const XT b = rhs_at<XT>(C, g, o.code, ps.x, ps.y, ps.z);
+        const float r32 = X::residual32(b, ax);
+        const float b32 = X::to_float(b);
         a_rr.add_prod(r32, r32);
         a_bb.add_prod(b32, b32);
         if constexpr (BICG) {
@@ -100,7 +137,7 @@ struct OpReplace {
     }
     __device__ void store(int64_t i, const Out &a, const Out &b, bool v0_, bool v1_)
     {
-        store2<FF>(x64n, i, a.x, b.x, v0_, v1_);
+        store2<XT>(x64n, i, a.x, b.x, v0_, v1_);
         store2<float>(r, i, a.r, b.r, v0_, v1_);
         if (restart) {
             store2<float>(p, i, 0.f, 0.f, v0_, v1_);
@@ -172,20 +209,23 @@ struct OpReplace {
 // stored, fp32(r64) goes to t, from which step 1 takes r_k (k1_mode = 1, e =
 // 0); on a restart it also becomes the shadow residual r0 and beta = 0 makes
 // p_k = r_k.  Dots (FP32-accumulated): |fp32(r64)|^2, |b|^2, r0.fp32(r64).
+// x64 and b - A x are FP64 by default, float-float on request (XArith).
 // Streams: x64, e, p, r, v, r0, code.
 // ===========================================================================
+template <typename XT>
 struct OpReplaceBi2 {
-    using T = FF;
+    using T = XT;
+    using X = XArith<XT>;
     using R = double;
     using SL = Streams<8, 4, 4, 4, 4, 4, 1>;
     static constexpr int NV = 3;
     using Shared = Coef<float>;
-    struct Vals { FF x; float e, p, r, v, r0; uint32_t code; };
+    struct Vals { XT x; float e, p, r, v, r0; uint32_t code; };
     struct Own { uint32_t code; float r0; };
-    struct Out { FF x; float r; };
+    struct Out { XT x; float r; };
     const CUtensorMap *tmap[SL::N];
     Faces<T> F;
-    FF *x64n;
+    XT *x64n;
     float *t, *r0;
     float alpha, omega;
     bool restart;
@@ -195,7 +235,7 @@ struct OpReplaceBi2 {
     __device__ static void load_shared(Shared &S, const Job &J, int tid) { load_coef<float>(S, J, tid); }
     __device__ static void load2(const unsigned char *st, const Pt &p_, Vals &a, Vals &b)
     {
-        sv2<FF, SL, 0>(st, p_, a.x, b.x);
+        sv2<XT, SL, 0>(st, p_, a.x, b.x);
         sv2<float, SL, 1>(st, p_, a.e, b.e);
         sv2<float, SL, 2>(st, p_, a.p, b.p);
         sv2<float, SL, 3>(st, p_, a.r, b.r);
@@ -205,7 +245,7 @@ struct OpReplaceBi2 {
     }
     __device__ static void load1(const unsigned char *st, const Pt &p_, Vals &a)
     {
-        a.x = sv<FF, SL, 0>(st, p_);
+        a.x = sv<XT, SL, 0>(st, p_);
         a.e = sv<float, SL, 1>(st, p_);
         a.p = sv<float, SL, 2>(st, p_);
         a.r = sv<float, SL, 3>(st, p_);
@@ -225,35 +265,35 @@ struct OpReplaceBi2 {
         tmap[4] = &J.tm[TM_V + par];
         tmap[5] = &J.tm[TM_R0];
         tmap[6] = &J.tm[TM_CODE];
-        x64n = (FF *)J.x64[cur ^ 1];
+        x64n = (XT *)J.x64[cur ^ 1];
         t = (float *)J.t;
         r0 = (float *)J.r0;
         alpha = (float)sc.alpha;
         omega = (float)sc.omega;
         restart = sc.replace == 2;
     }
-    __device__ FF iterate(const Geo &g, Shared &S, const Vals &a, const Pos &ps) const
+    __device__ XT iterate(const Geo &g, Shared &S, const Vals &a, const Pos &ps) const
     {
         const float inv = inv_of<float, true>(S, g, a.code, ps);
         const float ek = a.e + alpha * (a.p * inv) + omega * ((a.r - alpha * a.v) * inv);
-        return ff_add_f(a.x, ek);
+        return X::add_f(a.x, ek);
     }
-    __device__ FF field(const Geo &g, const Coef<FF> &, Shared &S, const Vals &a, const Pos &ps) const
+    __device__ XT field(const Geo &g, const typename X::Tab &, Shared &S, const Vals &a, const Pos &ps) const
     {
         return iterate(g, S, a, ps);
     }
-    __device__ Own own(const Geo &g, const Coef<FF> &, Shared &S, const Vals &a, const Pos &ps, FF &f) const
+    __device__ Own own(const Geo &g, const typename X::Tab &, Shared &S, const Vals &a, const Pos &ps, XT &f) const
     {
         f = iterate(g, S, a, ps);
         return Own{a.code, a.r0};
     }
-    __device__ Out apply(const Geo &g, const Coef<FF> &C, Shared &, const Own &o, const Pos &ps, FF fc, FF fxp,
-                         FF fxm, FF fyp, FF fym, FF fzp, FF fzm)
+    __device__ Out apply(const Geo &g, const typename X::Tab &C, Shared &, const Own &o, const Pos &ps, XT fc,
+                         XT fxp, XT fxm, XT fyp, XT fym, XT fzp, XT fzm)
     {
-        const FF ax = stencil7_ff(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag_ff(C, o.code, ps));
-        const FF b = rhs_at<FF>(C, g, o.code, ps.x, ps.y, ps.z);
-        const float r32 = ff_to_float(ff_add(b, ff_neg(ax)));
-        const float b32 = ff_to_float(b);
+        const XT ax = X::stencil(F, C, g, o.code, ps, fc, fxp, fxm, fyp, fym, fzp, fzm);
+        const XT b = rhs_at<XT>(C, g, o.code, ps.x, ps.y, ps.z);
+        const float r32 = X::residual32(b, ax);
+        const float b32 = X::to_float(b);
         a_rr.add_prod(r32, r32);
         a_bb.add_prod(b32, b32);
         a_d.add_prod(restart ? r32 : o.r0, r32);
@@ -261,7 +301,7 @@ struct OpReplaceBi2 {
     }
     __device__ void store(int64_t i, const Out &a, const Out &b, bool v0_, bool v1_)
     {
-        store2<FF>(x64n, i, a.x, b.x, v0_, v1_);
+        store2<XT>(x64n, i, a.x, b.x, v0_, v1_);
         store2<float>(t, i, a.r, b.r, v0_, v1_);
         if (restart) store2<float>(r0, i, a.r, b.r, v0_, v1_);
     }
@@ -389,7 +429,8 @@ __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
     const Job &J = L.jobs[s_job];
     const TileCoords t = tile_coords(J, tid);
     const Geo g{J.nx, J.ny, J.nz, J.dir >> 1, (J.dir & 1) ? -1 : 1, J.pitch};
-    FF *x64 = (FF *)J.x64[0];
+    void *x64 = J.x64[0];
+    const bool ff = J.x64_ff != 0;
     float *e = (float *)J.x;
     // Two-sweep BiCGSTAB: the first replacement reads r, p, v (scaled by
     // alpha = omega = 0) and step 1 reads t; all start at zero.
@@ -399,7 +440,9 @@ __global__ void __launch_bounds__(NTHREADS) init64_kernel(Launch L)
         for (int z = t.z0; z < t.z1; ++z) {
             const int64_t i = g.idx(t.gx + k, t.gy, z);
             if (!ft_in(J, i, i, (int64_t)J.pitch * J.ny * J.nz, OOB_INIT)) continue;
-            x64[i] = FF(x0_at<float>(g, t.gx + k, t.gy, z), 0.f);
+            const float x0 = x0_at<float>(g, t.gx + k, t.gy, z);
+            if (ff) ((FF *)x64)[i] = FF(x0, 0.f);
+            else ((double *)x64)[i] = (double)x0;
             e[i] = 0.f;
             if (zt) {
                 zr[i] = 0.f;

@@ -76,7 +76,19 @@ __device__ __forceinline__ uint64_t global_timer_ns()
     return t;
 }
 
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
+// Limit of every bounded wait; test builds shorten it.
+#ifndef FAST_TAU_WAIT_LIMIT_NS
+#define FAST_TAU_WAIT_LIMIT_NS 2000000000ull  // 2 s
+#endif
+constexpr uint64_t kWaitLimitNs = FAST_TAU_WAIT_LIMIT_NS;
+
+// FAST_TAU_TEST_HOOKS=1 builds (tests only) honour Scalars::test_withhold: the
+// first sweep of an armed right-hand side does not issue the tile loads of
+// plane 1 in its first tile, so that block's bounded wait runs out and the
+// solve fails with FAST_TIMEOUT.  Compiled out by default.
+#ifndef FAST_TAU_TEST_HOOKS
+#define FAST_TAU_TEST_HOOKS 0
+#endif
 
 // Waits for phase `parity` of the mbarrier, giving up after kWaitLimitNs.
 template <uint32_t HINT = 0>
@@ -312,6 +324,9 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
     __syncthreads();
     // Tile loads of plane pa+q into ring slot (qb + q) % NSTAGE (thread 0 only).
     auto issue = [&](int q) {
+#if FAST_TAU_TEST_HOOKS
+        if (q == 1 && local == 0 && atomicExch(&J.sc->test_withhold, 0) != 0) return;
+#endif
         const int st = (qb + q) % NSTAGE;
         const uint32_t bar = smem_u32(&bars[st]);
         mbar_arrive_expect_tx(bar, (uint32_t)SL::tx_bytes());
@@ -496,7 +511,15 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel_tiles(Launch L)
     for (int64_t blk = blockIdx.x; blk < L.nblocks;) {
         int64_t idle_end = 0;
         const int r = sweep_body<Op, NSTAGE>(L, blk, qb, ready, &idle_end);
-        if (r == SWEEP_FAULT) return;
+        if (r == SWEEP_FAULT) {
+            // The stage ring of this block is unusable now: the right-hand
+            // sides of the tiles it leaves undone cannot finish this step
+            // either, so they fail too (no partial reduction reaches them).
+            if (threadIdx.x == 0)
+                for (int64_t b = blk + gridDim.x; b < L.nblocks; b += gridDim.x)
+                    atomicExch(&L.jobs[find_job(L, b)].sc->state, (int32_t)FAULT);
+            return;
+        }
         if (r == SWEEP_IDLE && idle_end > blk + gridDim.x) {
             // first tile >= idle_end that belongs to this block
             blk += ((idle_end - blk + gridDim.x - 1) / gridDim.x) * gridDim.x;

@@ -80,6 +80,8 @@ struct Scalars {
                             // one-sweep CG: 1 = the next sweep restarts from the replaced residual
     int32_t cg_fused;       // 1: MIXED CG runs as one sweep per iteration (OpCGF)
     int32_t oob;            // bounds-check builds: first failing access site (0 = none)
+    int32_t test_withhold;  // test-hook builds: withhold one tile load of the next sweep (see tau_sweep.cuh)
+    int32_t pad_hook;
     // reductions for tau and porosity
     double flux_sum;    // sum over voxels of the tau flux term
     uint64_t pores;     // number of zero (pore) voxels
@@ -106,7 +108,8 @@ struct Job {
     void *p[2];                  // search direction ping-pong (T)
     void *v[2];                  // BiCGSTAB v ping-pong (T)
     void *t;                     // MIXED BiCGSTAB: t = A s, kept from step 2 to step 1 (FP32)
-    void *x64[2];                // MIXED extended-precision iterate ping-pong: float-float (hi, lo) pairs
+    void *x64[2];                // MIXED extended-precision iterate ping-pong: double, or float-float
+                                 // (hi, lo) pairs when x64_ff is set
     Scalars *sc;
     double *part;                // ntiles * NPART partial sums
     uint32_t *counter;           // finisher arrival counter
@@ -119,13 +122,13 @@ struct Job {
     float finv_b[7][128];        // 1/diag, FP32
     double ddiag_int[128];       // interior diagonal, FP64
     double dinv_int[128];        // 1/diag, FP64
-    // MIXED residual replacement: the FP64 values above as float-float
-    // pairs (value = hi + lo), the diagonal by (boundary count + 2, code).
+    // MIXED residual replacement in float-float (x64_ff): the FP64 values
+    // above as pairs (value = hi + lo), the diagonal by (boundary count + 2, code).
     float xdiag_hi[7][128], xdiag_lo[7][128];
     float xface[2][2][2];        // [self solid][neighbour solid][hi, lo]
     float xcell2[2][2];          // 2*D by solid bit, [hi, lo]
     float c_tau[2];              // tau cell coefficients (float coeffs of the reference)
-    int32_t inner_parity;        // unused, keeps alignment
+    int32_t x64_ff;              // MIXED: 1 = x64 holds float-float pairs, 0 = doubles
     int32_t pad0;
 };
 

@@ -105,6 +105,8 @@ class TortuosityParams:
     precision: Precision = Precision.F64
     face_mean: FaceMean = FaceMean.ARITHMETIC
     profile: bool = False      # time every kernel launch (see _native.last_stats)
+    # MIXED: float-float iterate and replacement residual instead of FP64 (opt-in)
+    replace_float_float: bool = False
 
     def to_c(self, solver: DiffusionSolverType) -> _native.fast_tau_params:
         p = _native.fast_tau_params()
@@ -118,7 +120,8 @@ class TortuosityParams:
         p.d1 = _f32(self.coeffs[1])
         p.porosity = float(self.porosity) if self.porosity_precomputed else -1.0
         p.verbose = 1 if self.verbose else 0
-        p.flags = _native.FLAG_PROFILE if self.profile else 0
+        p.flags = (_native.FLAG_PROFILE if self.profile else 0) | \
+            (_native.FLAG_REPLACE_FLOAT_FLOAT if self.replace_float_float else 0)
         return p
 
 

@@ -60,10 +60,10 @@ typedef enum fast_solver { FAST_SOLVER_BICGSTAB = 0, FAST_SOLVER_CG = 1 } fast_s
  * `-p float` (TauModule.h:19,125-129): the whole solve in that type.  MIXED is
  * the engine's fast path: FP32 Krylov iterations (FP32-accumulated,
  * block-compensated dot products) on a correction e of an FP64 iterate x;
- * whenever the FP32 recursive residual has fallen a decade, claims
- * convergence or breaks down, an FP64 step folds e into x, recomputes the true
- * residual b - A x in FP64 and hands it back to the recursion (residual
- * replacement, with a Krylov restart on breakdown).  Convergence is decided
+ * whenever the FP32 recursive residual has fallen well below its recent
+ * largest value, claims convergence or breaks down, an FP64 step folds e into
+ * x, recomputes the true residual b - A x in FP64 and hands it back to the
+ * recursion (residual replacement, with a Krylov restart on breakdown).  Convergence is decided
  * on the FP64 true residual; the tau flux integral is FP64. */
 typedef enum fast_precision { FAST_PREC_F64 = 0, FAST_PREC_F32 = 1, FAST_PREC_MIXED = 2 } fast_precision;
 
@@ -90,6 +90,10 @@ typedef struct fast_tau_params {
 /* fast_tau_params.flags: time every kernel launch of the solve with CUDA
  * events (launches are serialised and not graph-replayed while profiling). */
 #define FAST_FLAG_PROFILE 1
+/* MIXED only: keep the iterate as a float-float pair per voxel and evaluate
+ * the replacement's b - A x with error-free FP32 transformations (about 48
+ * significant bits) instead of FP64.  Off by default: FP64 is the contract. */
+#define FAST_FLAG_REPLACE_FLOAT_FLOAT 2
 
 /* Per-direction result. */
 typedef struct fast_tau_result {

@@ -83,21 +83,25 @@ def test_f32_matches_float_oracle(gpu, oracle, solver):
     assert rel(tau, ref["tau"]) <= 1e-4
 
 
+@pytest.mark.parametrize("ff", [False, True], ids=["x64_fp64", "x64_float_float"])
 @pytest.mark.parametrize("solver", [ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB])
-def test_mixed_within_1e5_of_fp64_oracle(gpu, oracle, solver):
+def test_mixed_within_1e5_of_fp64_oracle(gpu, oracle, solver, ff):
     mask = _vol((48, 40, 36), seed=9, frac=0.6, r=4.0)
     for d in (0, 3, 4):
-        p = ft.TortuosityParams(dir=ft.Dir(d), tolerance=1e-7, precision=ft.Precision.MIXED)
+        p = ft.TortuosityParams(dir=ft.Dir(d), tolerance=1e-7, precision=ft.Precision.MIXED,
+                                replace_float_float=ff)
         tau = ft.get_tortuosity(mask, p, solver)
         ref = oracle.get_tortuosity(mask, dir=d, solver=1, tol=1e-10)
         assert rel(tau, ref["tau"]) <= 1e-5, (d, tau, ref["tau"])
 
 
+@pytest.mark.parametrize("ff", [False, True], ids=["x64_fp64", "x64_float_float"])
 @pytest.mark.parametrize("solver", [ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB])
-def test_mixed_reaches_fp64_accuracy(gpu, oracle, solver):
+def test_mixed_reaches_fp64_accuracy(gpu, oracle, solver, ff):
     mask = _vol((40, 36, 44), seed=21, frac=0.55, r=3.5)
     for d in (1, 2, 5):
-        p = ft.TortuosityParams(dir=ft.Dir(d), tolerance=1e-10, precision=ft.Precision.MIXED)
+        p = ft.TortuosityParams(dir=ft.Dir(d), tolerance=1e-10, precision=ft.Precision.MIXED,
+                                replace_float_float=ff)
         res = ft.solve_directions(mask, [ft.Dir(d)], p, solver)[0]
         assert res.status == ft.Status.OK, res
         assert res.rel_residual <= 1e-10
@@ -196,6 +200,20 @@ def test_concentration_output(gpu, oracle):
     ft.get_tortuosity(mask, p, ft.DSOLVER_CG, concentration_output=conc)
     ref = oracle.get_tortuosity(mask, dir=5, solver=1, tol=1e-11, return_conc=True)
     assert np.max(np.abs(conc - ref["conc"])) < 1e-8
+
+
+@pytest.mark.parametrize("ff", [False, True], ids=["x64_fp64", "x64_float_float"])
+def test_mixed_concentration_output(gpu, oracle, ff):
+    """The MIXED iterate handed out as FP64 (read directly, or widened from
+    float-float pairs) equals the oracle's field at a tight tolerance."""
+    mask = _vol((16, 18, 20), seed=4)
+    p = ft.TortuosityParams(dir=ft.Dir.Y_NEG, tolerance=1e-10, precision=ft.Precision.MIXED,
+                            replace_float_float=ff)
+    conc = np.zeros(mask.shape, np.float64)
+    tau = ft.get_tortuosity(mask, p, ft.DSOLVER_BICGSTAB, concentration_output=conc)
+    ref = oracle.get_tortuosity(mask, dir=3, solver=1, tol=1e-11, return_conc=True)
+    assert rel(tau, ref["tau"]) <= 1e-8
+    assert np.max(np.abs(conc - ref["conc"])) < 1e-7
 
 
 def test_multi_direction_matches_single(gpu):
