@@ -436,6 +436,15 @@ def run_ours(args, ws, rank, local):
         line["alternatives"] = alt
     if cpu:
         line["cpu_baseline"] = cpu
+    if ws == 1 and not args.no_subrecords:
+        # the two other targets of the specification, measured in the same
+        # run: the 1024^3 PCG iteration against the HBM roofline, and the
+        # serving stream against the plain drop-in solver (a bounded sample of
+        # the 10,000-request stream: the first --c4-requests of its requests)
+        del d_mask
+        torch.cuda.empty_cache()
+        line["c5"] = c5_record(args.c5_edge)
+        line["c4"] = c4_record(args.c4_requests, args.c4_rates, args.c4_plain_sample)
     print(json.dumps(line), flush=True)
 
 
@@ -584,11 +593,13 @@ def run_c3(args):
     print(json.dumps(line), flush=True)
 
 
-def c4_requests(n, seed=2024):
+def c4_requests(n, seed=2024, pool=0):
     """Serving stream requests: edge log-uniform in [32, 384] (cubic),
     spheres (r U[3,8]) or ellipsoids (semi-major 8, aspect U[0.1,1.0]),
     solid fraction U[0.40,0.75], direction uniform over the six, CG or
-    BiCGSTAB."""
+    BiCGSTAB.  With pool > 0 only the first `pool` volumes are generated and
+    request k carries volume k % pool (with its own direction and solver), so
+    a long stream fits in host memory; the size mix is the pool's."""
     from concurrent.futures import ThreadPoolExecutor
     from fast_gb300 import volumes
     rng = np.random.default_rng(seed)
@@ -600,6 +611,11 @@ def c4_requests(n, seed=2024):
         aspect = float(rng.uniform(0.1, 1.0))
         specs.append(dict(edge=e, frac=frac, kind=kind, aspect=aspect, seed=int(rng.integers(1 << 30)),
                           dir=int(rng.integers(6)), solver=int(rng.integers(2))))
+    npool = n if pool <= 0 or pool >= n else pool
+    for k in range(npool, n):  # volume of request k: the pool's entry k % npool
+        src = specs[k % npool]
+        specs[k].update(edge=src["edge"], frac=src["frac"], kind=src["kind"], aspect=src["aspect"],
+                        seed=src["seed"])
 
     def gen(sp):
         sh = (sp["edge"],) * 3
@@ -607,25 +623,29 @@ def c4_requests(n, seed=2024):
             return volumes.spheres(sh, seed=sp["seed"], r_min=3.0, r_max=8.0, solid_fraction=sp["frac"])
         return volumes.ellipsoids(sh, sp["seed"], 8.0, sp["aspect"], sp["frac"])
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
-        masks = list(ex.map(gen, specs))
+        vols = list(ex.map(gen, specs[:npool]))
+    masks = [vols[k % npool] for k in range(n)]
     return specs, masks
 
 
-def run_c4(args):
-    """Serving stream: Poisson arrivals of c4_requests() at each rate of
-    --rates into one TauServer (MIXED, tol 1e-6); latency = completion minus
+def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0):
+    """Serving stream: Poisson arrivals of c4_requests(n_requests) at each
+    rate into one TauServer (MIXED, tol 1e-6); latency = completion minus
     arrival; against the plain drop-in solver (FP64, one request per call,
-    back to back) on the same requests."""
+    back to back) on the same requests (all, or `plain_sample` of them evenly
+    spaced through the stream so the sample keeps its size mix)."""
     import torch
     import fast_gb300 as ft
     from fast_gb300.serve import TauServer
-    specs, masks = c4_requests(args.requests)
+    t0g = time.perf_counter()
+    specs, masks = c4_requests(n_requests, pool=pool)
+    t_gen = time.perf_counter() - t0g
     out = {}
     rng = np.random.default_rng(7)
-    for rate in args.rates:
+    for rate in rates:
         gaps = rng.exponential(1.0 / rate, size=len(masks))
         arrivals = np.cumsum(gaps)
-        with TauServer(tolerance=1e-6, chunk=16) as srv:
+        with TauServer(tolerance=1e-6, chunk=chunk) as srv:
             t0 = srv.now()
             k = 0
             done = []
@@ -641,47 +661,56 @@ def run_c4(args):
             span = max(c.t_done for c in done) - (t0 + arrivals[0])
         by_ticket = sorted(done, key=lambda c: c.ticket)
         lat = [c.t_done - (t0 + arrivals[i]) for i, c in enumerate(by_ticket)]
-        out[str(rate)] = {"solves_per_s": len(done) / span, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
-                          "p99_ms": 1e3 * float(np.percentile(lat, 99)),
-                          "all_converged": all(c.result.status == ft.Status.OK for c in done)}
-    # plain drop-in, one request per call, on the same requests (or, with
-    # --plain-sample n, on n of them evenly spaced through the stream so that
-    # the sample keeps the stream's size mix)
+        out[str(int(rate))] = {"solves_per_s": len(done) / span, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                               "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                               "arrival_span_s": float(arrivals[-1] - arrivals[0]), "makespan_s": span,
+                               "all_converged": all(c.result.status == ft.Status.OK for c in done)}
     n = len(masks)
-    picks = list(range(n)) if args.plain_sample <= 0 or args.plain_sample >= n else \
-        sorted({int(i) for i in np.linspace(0, n - 1, args.plain_sample)})
-    q = {s: ft.TortuosityParams(tolerance=1e-6, precision=ft.Precision.F64) for s in (0, 1)}
+    picks = list(range(n)) if plain_sample <= 0 or plain_sample >= n else \
+        sorted({int(i) for i in np.linspace(0, n - 1, plain_sample)})
+    q = {s_: ft.TortuosityParams(tolerance=1e-6, precision=ft.Precision.F64) for s_ in (0, 1)}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in picks:
         ft.solve_directions(masks[k], [ft.Dir(specs[k]["dir"])], q[specs[k]["solver"]],
                             ft.DiffusionSolverType(specs[k]["solver"]))
     plain = len(picks) / (time.perf_counter() - t0)
-    nplain = len(picks)
     best = max(v["solves_per_s"] for v in out.values())
     voxels = [m.size for m in masks]
+    return {"requests": n, "distinct_volumes": (pool if 0 < pool < n else n), "rates": out,
+            "best_solves_per_s": best,
+            "plain_dropin_f64_solves_per_s": plain, "plain_sample": len(picks),
+            "speedup_vs_plain_f64": best / plain,
+            "voxels_per_request": {"mean": float(np.mean(voxels)), "max": int(max(voxels)),
+                                   "plain_sample_mean": float(np.mean([voxels[k] for k in picks]))},
+            "generation_seconds": t_gen,
+            "mix": "edge log-U[32,384] cubic, spheres r U[3,8] or ellipsoids aspect U[0.1,1], "
+                   "solid U[0.40,0.75], dir U(6), CG or BiCGSTAB",
+            "server": "TauServer MIXED tol 1e-6, 16-iteration chunks, admission by HBM footprint"}
+
+
+def run_c4(args):
+    import fast_gb300  # noqa: F401
+    rec = c4_record(args.requests, args.rates, args.plain_sample, pool=args.c4_pool)
+    best = rec["best_solves_per_s"]
     line = _line("tau solves/s", best, "solves/s", args, 1e3 / best, "f32+f64",
-                 {"workload": "c4_serving_stream", "requests": len(masks),
-                  "mix": "edge log-U[32,384] cubic, spheres r U[3,8] or ellipsoids aspect U[0.1,1], "
-                         "solid U[0.40,0.75], dir U(6), CG or BiCGSTAB", "tol": 1e-6,
-                  "server": "TauServer MIXED, 16-iteration chunks, admission by HBM footprint"},
-                 rates=out, plain_dropin_f64_solves_per_s=plain, plain_sample=nplain,
-                 speedup_vs_plain_f64=best / plain,
-                 voxels_per_request={"mean": float(np.mean(voxels)), "max": int(max(voxels)),
-                                     "plain_sample_mean": float(np.mean([voxels[k] for k in picks]))})
+                 {"workload": "c4_serving_stream", "requests": rec["requests"], "mix": rec["mix"], "tol": 1e-6,
+                  "server": rec["server"]}, **{k: v for k, v in rec.items() if k not in ("mix", "server")})
     print(json.dumps(line), flush=True)
 
 
-def run_c5(args):
-    """Large volume: 1024^3 spheres (seed 7, r = 10, solid 0.65); GPU CCL of
-    the pore phase (label count, components spanning x, canonical-order check
-    of the labels on the device), then MIXED Jacobi-PCG in x to tol 1e-6,
-    reported as algorithmic GB/s (25 B per voxel-iteration) against the
-    measured HBM peak; tau compared with a MIXED solve to tol 1e-9."""
+def c5_record(edge=1024, reference=False):
+    """Large volume: edge^3 spheres (seed 7, r = 10, solid 0.65); GPU CCL of
+    the pore phase (label count against the oracle's, components spanning
+    x, canonical order checked on the device), then MIXED Jacobi-PCG in x to
+    tol 1e-6, timed with CUDA events, and once more with every kernel timed:
+    the iteration kernels' algorithmic GB/s (25 B per voxel-iteration)
+    against the measured HBM peak, and tau against the FP64 tau of the golden
+    record (GPU FP64 PCG, tol 1e-10)."""
     import torch
     import fast_gb300 as ft
     from fast_gb300 import _native, ccl, volumes
-    n = args.c5_edge
+    n = edge
     t0 = time.perf_counter()
     m = volumes.spheres((n, n, n), seed=7, r_min=10.0, solid_fraction=0.65)
     t_gen = time.perf_counter() - t0
@@ -691,12 +720,13 @@ def run_c5(args):
     d_labels = torch.empty((n, n, n), dtype=torch.int32, device="cuda")
     ccl.get_volume_ccl_device(d_mask.data_ptr(), (n, n, n), d_labels.data_ptr(), background=255, boundary=False)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    e0, e1 = _events(stream)
+    e0.record(stream)
     c = ccl.get_volume_ccl_device(d_mask.data_ptr(), (n, n, n), d_labels.data_ptr(), background=255)
+    e1.record(stream)
     torch.cuda.synchronize()
-    t_ccl = time.perf_counter() - t0
+    ms_ccl = e0.elapsed_time(e1)
     lab = d_labels.view(-1)
-    # canonical numbering: first occurrence of label k+1 after that of label k
     fg = lab != 0
     first = torch.full((c.num_labels,), lab.numel(), dtype=torch.int64, device="cuda")
     idx = torch.nonzero(fg).squeeze(1)
@@ -708,9 +738,14 @@ def run_c5(args):
     span_vox = int(sizes[torch.from_numpy(spanning.astype(bool)).cuda()].sum().item())
     del first, idx, fg, sizes, lab, d_labels
     torch.cuda.empty_cache()
+    golden = None
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "workloads.json")) as f:
+            golden = json.load(f)["workloads"].get(f"spheres{n}")
+    except Exception:
+        golden = None
 
     p = ft.TortuosityParams(tolerance=1e-6, max_iter=100000, precision=ft.Precision.MIXED)
-    e0, e1 = _events(stream)
     e0.record(stream)
     res = ft.solve_directions_device(d_mask.data_ptr(), (n, n, n), [ft.Dir.X_POS], p, ft.DSOLVER_CG,
                                      stream=stream.cuda_stream)[0]
@@ -726,29 +761,47 @@ def run_c5(args):
     gbs = 25.0 * N * res.iterations / (iter_ms / 1e3) / 1e9
     sweep_ms = sum(prof.get(k, {"ms": 0})["ms"] for k in ("cg1", "cg2"))
     dram_gbs = C5_DRAM_BYTES_PER_VOXEL_ITER * N * res.iterations / (sweep_ms / 1e3) / 1e9
+    per_kernel = {}
+    for k, b in (("cg1", 13), ("cg2", 21)):
+        if k in prof and prof[k]["ms"] > 0:
+            per_kernel[k] = {"bytes_per_voxel": b, "ms_per_launch": prof[k]["ms"] / max(prof[k]["launches"], 1),
+                             "gbs": b * N * res.iterations / (prof[k]["ms"] / 1e3) / 1e9}
     peak, kind = load_peaks()
-    ref = None
-    if not args.c5_no_reference:
+    rec = {"volume": f"{n}^3 spheres seed 7 r=10 solid 0.65", "solver": "MIXED Jacobi-PCG, x, tol 1e-6",
+           "solve_ms": ms, "solves_per_s": 1e3 / ms, "tau": res.tau, "iterations": res.iterations,
+           "status": int(res.status), "outer_steps": res.outer_steps,
+           "stencil_iteration": {"gbs_at_25B": gbs, "peak": peak, "peak_kind": kind, "frac": gbs / peak,
+                                 "frac_of_8000": gbs / 8000.0, "iteration_ms": iter_ms / max(res.iterations, 1),
+                                 "dram_gbs": dram_gbs, "dram_frac": dram_gbs / peak,
+                                 "dram_bytes_per_voxel_iter": C5_DRAM_BYTES_PER_VOXEL_ITER,
+                                 "kernels": per_kernel,
+                                 "kernel_ms": {k: round(v["ms"], 2) for k, v in prof.items()}},
+           "ccl": {"ms": ms_ccl, "num_labels": c.num_labels, "canonical_order": canonical, "pore_voxels": pores,
+                   "x_spanning_components": int(spanning[1:].sum()),
+                   "x_spanning_pore_fraction": span_vox / max(pores, 1),
+                   "num_labels_equals_oracle": (c.num_labels == golden["ccl"]["num_labels"]) if golden else None},
+           "generation_seconds": t_gen}
+    if golden and "0" in golden.get("dirs", {}):
+        ref = golden["dirs"]["0"]["tau_cg_1e-10"]
+        rec["tau_fp64_1e-10"] = ref
+        rec["dtau_rel_vs_fp64"] = abs(res.tau - ref) / ref
+        rec["fp64_reference"] = golden["dirs"]["0"].get("solver_cg_1e-10")
+    if reference:
         q = ft.TortuosityParams(tolerance=1e-9, max_iter=200000, precision=ft.Precision.MIXED)
-        ref = ft.solve_directions_device(d_mask.data_ptr(), (n, n, n), [ft.Dir.X_POS], q, ft.DSOLVER_CG,
-                                         stream=stream.cuda_stream)[0]
-    line = _line("tau solves/s", 1e3 / ms, "solves/s", args, ms, "f32+f64",
-                 {"workload": f"c5_spheres{n}_x_cg_mixed", "volume": f"{n}^3 spheres seed 7 r=10 solid 0.65",
-                  "solver": "Jacobi-PCG", "tol": 1e-6},
-                 tau=res.tau, iterations=res.iterations, status=int(res.status),
-                 stencil_iteration={"gbs_at_25B": gbs, "peak": peak, "peak_kind": kind, "frac": gbs / peak,
-                                    "frac_of_8000": gbs / 8000.0,
-                                    "dram_gbs": dram_gbs, "dram_frac": dram_gbs / peak,
-                                    "dram_frac_of_8000": dram_gbs / 8000.0,
-                                    "dram_bytes_per_voxel_iter": C5_DRAM_BYTES_PER_VOXEL_ITER,
-                                    "kernel_ms": {k: round(v["ms"], 2) for k, v in prof.items()}},
-                 ccl={"seconds": t_ccl, "num_labels": c.num_labels, "canonical_order": canonical,
-                      "pore_voxels": pores, "x_spanning_components": int(spanning[1:].sum()),
-                      "x_spanning_pore_fraction": span_vox / max(pores, 1)},
-                 generation_seconds=t_gen,
-                 tau_ref_mixed_1e9=(ref.tau if ref else None),
-                 dtau_rel_vs_1e9=(abs(res.tau - ref.tau) / ref.tau if ref else None),
-                 ref_iterations=(ref.iterations if ref else None))
+        r9 = ft.solve_directions_device(d_mask.data_ptr(), (n, n, n), [ft.Dir.X_POS], q, ft.DSOLVER_CG,
+                                        stream=stream.cuda_stream)[0]
+        rec["tau_mixed_1e-9"] = r9.tau
+        rec["dtau_rel_vs_mixed_1e-9"] = abs(res.tau - r9.tau) / r9.tau
+    del d_mask
+    torch.cuda.empty_cache()
+    return rec
+
+
+def run_c5(args):
+    rec = c5_record(args.c5_edge, reference=not args.c5_no_reference)
+    line = _line("tau solves/s", rec["solves_per_s"], "solves/s", args, rec["solve_ms"], "f32+f64",
+                 {"workload": f"c5_spheres{args.c5_edge}_x_cg_mixed", "volume": rec["volume"],
+                  "solver": "Jacobi-PCG", "tol": 1e-6}, **rec)
     print(json.dumps(line), flush=True)
 
 
@@ -876,12 +929,20 @@ def main():
     ap.add_argument("--ncu-precision", default=None, choices=["f64", "f32", "mixed"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "alpha"],
                     help="c2 (default) is the headline; the others print their own line")
-    ap.add_argument("--requests", type=int, default=64, help="c4: requests in the stream")
-    ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 2000.0], help="c4: arrival rates (1/s)")
-    ap.add_argument("--plain-sample", type=int, default=0,
-                    help="c4: requests timed on the plain solver (0: all of them)")
+    ap.add_argument("--requests", type=int, default=10000, help="c4: requests in the stream")
+    ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0, 2000.0],
+                    help="c4: arrival rates (1/s)")
+    ap.add_argument("--plain-sample", type=int, default=200,
+                    help="c4: requests timed on the plain solver, evenly spaced (0: all of them)")
     ap.add_argument("--c5-edge", type=int, default=1024)
     ap.add_argument("--c5-no-reference", action="store_true")
+    ap.add_argument("--no-subrecords", action="store_true",
+                    help="headline only: skip the large-volume (c5) and serving (c4) records of the default line")
+    ap.add_argument("--c4-requests", type=int, default=200, help="requests of the serving record in the default line")
+    ap.add_argument("--c4-rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0, 2000.0])
+    ap.add_argument("--c4-plain-sample", type=int, default=24)
+    ap.add_argument("--c4-pool", type=int, default=500,
+                    help="c4: distinct volumes generated for the stream (request k uses volume k %% pool)")
     ap.add_argument("--replica-check", action="store_true",
                     help="start the ranks, meet in a barrier and a max over ranks, print them and exit")
     args = ap.parse_args()

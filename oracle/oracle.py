@@ -85,6 +85,13 @@ def lib():
     return _lib
 
 
+def build_ref() -> None:
+    """Compile the reference's own assembly rule into oracle/_ref/ where the
+    reference's source tree is present (the Makefile's `ref-if-present`);
+    elsewhere this does nothing."""
+    subprocess.run(["make", "-s", "-C", _HERE, "ref-if-present"], check=True)
+
+
 def _volgen():
     """libvolgen.so: the seeded generator without the CUDA library."""
     global _gen
