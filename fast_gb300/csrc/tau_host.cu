@@ -90,6 +90,7 @@ int Engine::init(int dev)
     device = dev;
     CU(cudaSetDevice(dev));
     CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     CU(cudaMallocHost(&h_sc, sizeof(Scalars) * 2 * kMaxJobs));
     CU(cudaMallocHost(&h_jobs, sizeof(Job) * 2 * kMaxJobs));  // jobs + one code job per volume
     cudaError_t ce = configure_f64();
@@ -303,6 +304,87 @@ int tensor_map(CUtensorMap *tm, const void *base, int es, int64_t nx, int64_t ny
     return FAST_OK;
 }
 
+bool is_replace(Step s)
+{
+    return s == Step::REPLACE_CG || s == Step::REPLACE_BI || s == Step::REPLACE_CG_FF || s == Step::REPLACE_BI_FF;
+}
+
+// Captures `chunk` iterations of `steps` on `st` into an executable graph.
+// A MIXED iteration's residual-replacement step becomes a conditional (IF)
+// node whose body is the replacement kernel and a one-thread reset kernel:
+// the sweeps open it from the device (cudaGraphSetConditional) when a
+// right-hand side asks for a replacement, so the idle slot costs no launch.
+// The condition defaults to open at every replay of the graph, so a request
+// made in the last iteration of a chunk is served at the head of the next.
+// L.cond_flag (two device words, zero) must be set for the conditional form;
+// FAST_TAU_COND_REPLACE=0 captures the plain launch instead.
+int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const std::vector<Step> &steps, int chunk,
+                  void (*launch)(Step, const Launch &, cudaStream_t), cudaGraphExec_t *exec, bool *used_cond)
+{
+    bool cond = L0.cond_flag != nullptr && side != nullptr && env_int("FAST_TAU_COND_REPLACE", 1) != 0;
+    bool any = false;
+    for (Step s : steps) any |= is_replace(s);
+    cond = cond && any;
+    *used_cond = cond;
+    Launch L = L0;
+    L.cond = 0ull;
+    cudaGraph_t graph = nullptr;
+    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    cudaStreamCaptureStatus cst;
+    if (cond) {
+        cudaGraph_t g = nullptr;
+        e = cudaStreamGetCaptureInfo(st, &cst, nullptr, &g, nullptr, nullptr, nullptr);
+        cudaGraphConditionalHandle h = 0;
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+        L.cond = (unsigned long long)h;
+    }
+    for (int c = 0; c < chunk && e == cudaSuccess; c++) {
+        for (Step s : steps) {
+            if (!(cond && is_replace(s))) {
+                launch(s, L, st);
+                continue;
+            }
+            cudaGraph_t g = nullptr;
+            const cudaGraphNode_t *deps = nullptr;
+            const cudaGraphEdgeData *edges = nullptr;
+            size_t ndeps = 0;
+            e = cudaStreamGetCaptureInfo(st, &cst, nullptr, &g, &deps, &edges, &ndeps);
+            if (e != cudaSuccess) break;
+            cudaGraphNodeParams np{};
+            memset(static_cast<void *>(&np), 0, sizeof(np));
+            np.type = cudaGraphNodeTypeConditional;
+            np.conditional.handle = (cudaGraphConditionalHandle)L.cond;
+            np.conditional.type = cudaGraphCondTypeIf;
+            np.conditional.size = 1;
+            cudaGraphNode_t node = nullptr;
+            e = cudaGraphAddNode(&node, g, deps, edges, ndeps, &np);
+            if (e != cudaSuccess) break;
+            e = cudaStreamBeginCaptureToGraph(side, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) break;
+            launch(s, L, side);
+            launch_cond_reset(L, side);
+            cudaGraph_t body = nullptr;
+            e = cudaStreamEndCapture(side, &body);
+            if (e != cudaSuccess) break;
+            e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+            if (e != cudaSuccess) break;
+        }
+    }
+    cudaError_t ee = cudaStreamEndCapture(st, &graph);
+    if (e == cudaSuccess) e = ee;
+    if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return fail(FAST_CUDA_ERROR, "graph capture failed: %s", cudaGetErrorString(e));
+    }
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(FAST_CUDA_ERROR, "graph instantiate failed: %s", cudaGetErrorString(e));
+    return FAST_OK;
+}
+
 // Replays `chunk` iterations from a captured graph until every job has left
 // RUNNING; polls the device scalars one chunk behind so the queue never
 // drains while the host waits.
@@ -351,16 +433,11 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
         }
         return FAST_OK;
     }
-    cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int c = 0; c < chunk; c++)
-        for (Step s : steps) launch(s, L, st);
-    cudaError_t cerr = cudaStreamEndCapture(st, &graph);
-    if (cerr != cudaSuccess) return fail(FAST_CUDA_ERROR, "graph capture failed: %s", cudaGetErrorString(cerr));
-    cerr = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (cerr != cudaSuccess) return fail(FAST_CUDA_ERROR, "graph instantiate failed: %s", cudaGetErrorString(cerr));
+    bool cond = false;
+    int cs = capture_chunk(st, E.side, L, steps, chunk, launch, &exec, &cond);
+    if (cs != FAST_OK) return cs;
+    cudaError_t cerr = cudaSuccess;
 
     cudaEvent_t ev[2];
     cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
@@ -372,8 +449,11 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
         cerr = cudaGraphLaunch(exec, st);
         if (cerr != cudaSuccess) { status = fail(FAST_CUDA_ERROR, "graph launch: %s", cudaGetErrorString(cerr)); break; }
         t_prof.st.graph_replays += 1;
-        t_prof.st.launches += (uint64_t)chunk * steps.size();
-        for (Step s : steps) t_prof.st.kernel_launches[kind_of(s)] += (uint64_t)chunk;
+        for (Step s : steps) {
+            if (cond && is_replace(s)) continue;  // counted from the device below
+            t_prof.st.launches += (uint64_t)chunk;
+            t_prof.st.kernel_launches[kind_of(s)] += (uint64_t)chunk;
+        }
         Scalars *hb = E.h_sc + (k & 1) * Engine::kMaxJobs;
         cudaMemcpyAsync(hb, d_sc, sizeof(Scalars) * njobs, cudaMemcpyDeviceToHost, st);
         cudaEventRecord(ev[k & 1], st);
@@ -387,6 +467,15 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
     }
     cerr = cudaStreamSynchronize(st);
     if (cerr != cudaSuccess && status == FAST_OK) status = fail(FAST_CUDA_ERROR, "solver: %s", cudaGetErrorString(cerr));
+    if (cond && cerr == cudaSuccess) {
+        // conditional replacement slots that ran: the replacement kernel and
+        // the slot's reset kernel each
+        uint32_t bodies = 0;
+        if (cudaMemcpy(&bodies, L.cond_flag + 1, sizeof(bodies), cudaMemcpyDeviceToHost) == cudaSuccess) {
+            t_prof.st.launches += 2ull * bodies;
+            t_prof.st.kernel_launches[FAST_K_REPLACE] += bodies;
+        }
+    }
     cudaEventDestroy(ev[0]);
     cudaEventDestroy(ev[1]);
     cudaGraphExecDestroy(exec);
@@ -552,7 +641,7 @@ size_t solve_bytes(const std::vector<VolSpec> &vols, const std::vector<JobSpec> 
     for (const JobSpec &j : jobs) need += job_bytes(vols[j.vol].nx, vols[j.vol].ny, vols[j.vol].nz, prec, solver, zc);
     const size_t nj = jobs.size(), nv = vols.size();
     need += align_up(sizeof(Scalars) * nj, 256) + align_up(sizeof(uint32_t) * nj, 256) +
-            align_up(sizeof(Job) * (nj + nv), 256);
+            align_up(sizeof(Job) * (nj + nv), 256) + 256;  // + the replacement slot's condition words
     return need;
 }
 
@@ -691,6 +780,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     Scalars *d_sc = (Scalars *)A.take(sizeof(Scalars) * nj);
     uint32_t *d_cnt = (uint32_t *)A.take(sizeof(uint32_t) * nj);
     Job *d_jobs = (Job *)A.take(sizeof(Job) * (nj + nv));  // jobs, then one code job per volume
+    uint32_t *d_cond = (uint32_t *)A.take(2 * sizeof(uint32_t));  // replacement slot: [0] elector, [1] bodies run
     std::vector<uint8_t *> d_code(nv);
     std::vector<int> first_job(nv, -1);
     for (int v = 0; v < nv; v++) {
@@ -733,11 +823,12 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     CU(cudaMemcpyAsync(d_jobs, hj, sizeof(Job) * (nj + nv), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_sc, hs, sizeof(Scalars) * nj, cudaMemcpyHostToDevice, st));
     CU(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t) * nj, st));
+    CU(cudaMemsetAsync(d_cond, 0, 2 * sizeof(uint32_t), st));
     // The staging buffers are reused below: wait for the copies to land.
     CU(cudaStreamSynchronize(st));
 
-    Launch L{d_jobs, nj, 0, tile_base};
-    Launch LC{d_jobs + nj, nv, 0, code_base};
+    Launch L{d_jobs, nj, 0, tile_base, 0ull, d_cond};
+    Launch LC{d_jobs + nj, nv, 0, code_base, 0ull, nullptr};
 
     int status = FAST_OK;
     launch_counted(FAST_K_CODE, st, [&] { launch_code(LC, st); });

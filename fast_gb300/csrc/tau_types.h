@@ -137,6 +137,11 @@ struct Launch {
     int32_t njobs;
     int32_t pad;
     int64_t nblocks;    // total blocks = sum of job tiles
+    // Captured MIXED iterations: the graph's conditional handle of the
+    // residual-replacement slot (0: no conditional; the slot is launched
+    // every iteration) and a device word that elects one setter per epoch.
+    unsigned long long cond;
+    uint32_t *cond_flag;
 };
 
 }  // namespace ft
