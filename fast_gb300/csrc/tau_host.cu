@@ -318,25 +318,26 @@ bool is_replace(Step s)
 // made in the last iteration of a chunk is served at the head of the next.
 // L.cond_flag (two device words, zero) must be set for the conditional form;
 // FAST_TAU_COND_REPLACE=0 captures the plain launch instead.
-int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const std::vector<Step> &steps, int chunk,
-                  void (*launch)(Step, const Launch &, cudaStream_t), cudaGraphExec_t *exec, bool *used_cond)
+static cudaError_t capture_attempt(cudaStream_t st, cudaStream_t side, const Launch &L0, const std::vector<Step> &steps,
+                                   int chunk, void (*launch)(Step, const Launch &, cudaStream_t), bool cond,
+                                   cudaGraph_t *graph, const char **where)
 {
-    bool cond = L0.cond_flag != nullptr && side != nullptr && env_int("FAST_TAU_COND_REPLACE", 1) != 0;
-    bool any = false;
-    for (Step s : steps) any |= is_replace(s);
-    cond = cond && any;
-    *used_cond = cond;
     Launch L = L0;
     L.cond = 0ull;
-    cudaGraph_t graph = nullptr;
-    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaSuccess;
+    *graph = nullptr;
+    *where = "begin capture";
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
     cudaStreamCaptureStatus cst;
     if (cond) {
         cudaGraph_t g = nullptr;
+        *where = "capture info";
         e = cudaStreamGetCaptureInfo(st, &cst, nullptr, &g, nullptr, nullptr, nullptr);
         cudaGraphConditionalHandle h = 0;
-        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) {
+            *where = "conditional handle";
+            e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+        }
         L.cond = (unsigned long long)h;
     }
     for (int c = 0; c < chunk && e == cudaSuccess; c++) {
@@ -349,6 +350,7 @@ int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const st
             const cudaGraphNode_t *deps = nullptr;
             const cudaGraphEdgeData *edges = nullptr;
             size_t ndeps = 0;
+            *where = "capture dependencies";
             e = cudaStreamGetCaptureInfo(st, &cst, nullptr, &g, &deps, &edges, &ndeps);
             if (e != cudaSuccess) break;
             cudaGraphNodeParams np{};
@@ -358,8 +360,10 @@ int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const st
             np.conditional.type = cudaGraphCondTypeIf;
             np.conditional.size = 1;
             cudaGraphNode_t node = nullptr;
+            *where = "conditional node";
             e = cudaGraphAddNode(&node, g, deps, edges, ndeps, &np);
             if (e != cudaSuccess) break;
+            *where = "capture of the conditional body";
             e = cudaStreamBeginCaptureToGraph(side, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal);
             if (e != cudaSuccess) break;
@@ -368,16 +372,54 @@ int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const st
             cudaGraph_t body = nullptr;
             e = cudaStreamEndCapture(side, &body);
             if (e != cudaSuccess) break;
+            *where = "capture dependency update";
             e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
             if (e != cudaSuccess) break;
         }
     }
-    cudaError_t ee = cudaStreamEndCapture(st, &graph);
+    cudaError_t ee = cudaStreamEndCapture(st, graph);
+    if (e == cudaSuccess && ee != cudaSuccess) *where = "end capture";
     if (e == cudaSuccess) e = ee;
-    if (e != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess && *graph) {
+        cudaGraphDestroy(*graph);
+        *graph = nullptr;
+    }
+    return e;
+}
+
+// Captures `chunk` iterations of `steps` on `st` into an executable graph.
+// A MIXED iteration's residual-replacement step becomes a conditional (IF)
+// node whose body is the replacement kernel and a one-thread reset kernel:
+// the sweeps open it from the device (cudaGraphSetConditional) when a
+// right-hand side asks for a replacement, so the idle slot costs no launch.
+// The condition defaults to open at every replay of the graph, so a request
+// made in the last iteration of a chunk is served at the head of the next.
+// L.cond_flag (two device words, zero) must be set for the conditional form;
+// FAST_TAU_COND_REPLACE=0 captures the plain launch instead, and so does a
+// driver that refuses the conditional node (the reason is printed with
+// FAST_TAU_TRACE=1).
+int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const std::vector<Step> &steps, int chunk,
+                  void (*launch)(Step, const Launch &, cudaStream_t), cudaGraphExec_t *exec, bool *used_cond)
+{
+    bool cond = L0.cond_flag != nullptr && side != nullptr && env_int("FAST_TAU_COND_REPLACE", 1) != 0;
+    bool any = false;
+    for (Step s : steps) any |= is_replace(s);
+    cond = cond && any;
+    cudaGraph_t graph = nullptr;
+    const char *where = "";
+    cudaError_t e = capture_attempt(st, side, L0, steps, chunk, launch, cond, &graph, &where);
+    if (e != cudaSuccess && cond) {
+        if (env_int("FAST_TAU_TRACE", 0))
+            fprintf(stderr, "fasttau: conditional replacement slot not captured (%s: %s); plain slot used\n", where,
+                    cudaGetErrorString(e));
         cudaGetLastError();
-        return fail(FAST_CUDA_ERROR, "graph capture failed: %s", cudaGetErrorString(e));
+        cond = false;
+        e = capture_attempt(st, side, L0, steps, chunk, launch, false, &graph, &where);
+    }
+    *used_cond = cond;
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(FAST_CUDA_ERROR, "graph capture failed (%s): %s", where, cudaGetErrorString(e));
     }
     e = cudaGraphInstantiate(exec, graph, 0);
     cudaGraphDestroy(graph);
