@@ -57,17 +57,18 @@ cudaError_t configure_misc()
     return cudaSuccess;
 }
 
-// The last node of the conditional replacement slot: close the slot for the
-// next iteration (the sweeps reopen it when a right-hand side asks) and count
-// the slots that ran (flag[1]).
-__global__ void cond_reset_kernel(unsigned long long cond, uint32_t *flag)
+// The last node of a conditional replacement slot: re-arm the slot's
+// election word for the next replay and count the slot bodies that ran.
+__global__ void cond_reset_kernel(uint32_t *elector, uint32_t *count)
 {
-    flag[0] = 0u;
-    flag[1] += 1u;
-    cudaGraphSetConditional((cudaGraphConditionalHandle)cond, 0u);
+    *elector = 0u;
+    *count += 1u;
 }
 
-void launch_cond_reset(const Launch &L, cudaStream_t st) { cond_reset_kernel<<<1, 1, 0, st>>>(L.cond, L.cond_flag); }
+void launch_cond_reset(uint32_t *elector, uint32_t *count, cudaStream_t st)
+{
+    cond_reset_kernel<<<1, 1, 0, st>>>(elector, count);
+}
 
 void launch_init64(const Launch &L, cudaStream_t st) { init64_kernel<<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L); }
 

@@ -447,12 +447,12 @@ int create(const fast_ctx_config &cfg, Ctx **out)
         cudaMallocAsync((void **)&C->d_tmp[0], sizeof(Job) * K, C->st) != cudaSuccess ||
         cudaMallocAsync((void **)&C->d_tmp[1], sizeof(Job) * K, C->st) != cudaSuccess ||
         cudaMallocAsync((void **)&C->d_tmp[2], sizeof(Job) * K, C->st) != cudaSuccess ||
-        cudaMallocAsync((void **)&C->groups[0].d_cond, 2 * sizeof(uint32_t), C->st) != cudaSuccess ||
-        cudaMallocAsync((void **)&C->groups[1].d_cond, 2 * sizeof(uint32_t), C->st) != cudaSuccess)
+        cudaMallocAsync((void **)&C->groups[0].d_cond, kCondWords * sizeof(uint32_t), C->st) != cudaSuccess ||
+        cudaMallocAsync((void **)&C->groups[1].d_cond, kCondWords * sizeof(uint32_t), C->st) != cudaSuccess)
         return fin(ft_fail(FAST_NOMEM, "context tables"));
     if (cudaMemsetAsync(C->d_cnt, 0, sizeof(uint32_t) * K, C->st) != cudaSuccess ||
-        cudaMemsetAsync(C->groups[0].d_cond, 0, 2 * sizeof(uint32_t), C->st) != cudaSuccess ||
-        cudaMemsetAsync(C->groups[1].d_cond, 0, 2 * sizeof(uint32_t), C->st) != cudaSuccess ||
+        cudaMemsetAsync(C->groups[0].d_cond, 0, kCondWords * sizeof(uint32_t), C->st) != cudaSuccess ||
+        cudaMemsetAsync(C->groups[1].d_cond, 0, kCondWords * sizeof(uint32_t), C->st) != cudaSuccess ||
         cudaMallocHost(&C->h_snap[0], sizeof(Scalars) * K) != cudaSuccess ||
         cudaMallocHost(&C->h_snap[1], sizeof(Scalars) * K) != cudaSuccess ||
         cudaMallocHost(&C->h_init, sizeof(Scalars) * K) != cudaSuccess ||

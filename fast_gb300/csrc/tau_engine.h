@@ -80,6 +80,10 @@ void dispatch_mixed(Step s, const Launch &L, cudaStream_t st);
 // classic two with FAST_TAU_CG_FUSED=0).
 bool cg_fused_enabled();
 bool is_replace(Step s);
+// Device words of a chunk graph's conditional replacement slots (election
+// words of up to 63 slots, then the count of slot bodies that ran).
+constexpr int kCondWords = 64 + 1;
+uint32_t cond_bodies_run(const uint32_t *words);
 // Captures `chunk` iterations of `steps` into an executable graph, the MIXED
 // replacement slot as a conditional node when L.cond_flag is set.
 int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L, const std::vector<Step> &steps, int chunk,

@@ -318,6 +318,10 @@ bool is_replace(Step s)
 // made in the last iteration of a chunk is served at the head of the next.
 // L.cond_flag (two device words, zero) must be set for the conditional form;
 // FAST_TAU_COND_REPLACE=0 captures the plain launch instead.
+// Words of a chunk graph's conditional replacement slots: one election word
+// per slot, then the count of slot bodies that ran.
+constexpr int kMaxCondSlots = 63;
+
 static cudaError_t capture_attempt(cudaStream_t st, cudaStream_t side, const Launch &L0, const std::vector<Step> &steps,
                                    int chunk, void (*launch)(Step, const Launch &, cudaStream_t), bool cond,
                                    cudaGraph_t *graph, const char **where)
@@ -329,21 +333,29 @@ static cudaError_t capture_attempt(cudaStream_t st, cudaStream_t side, const Lau
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
     cudaStreamCaptureStatus cst;
+    // One handle per slot (a handle belongs to one conditional node): slot 0
+    // defaults to open at every replay (it serves requests made in the last
+    // iteration of the previous replay), the others to closed.
+    std::vector<cudaGraphConditionalHandle> h(cond ? chunk : 0, 0);
     if (cond) {
         cudaGraph_t g = nullptr;
         *where = "capture info";
         e = cudaStreamGetCaptureInfo(st, &cst, nullptr, &g, nullptr, nullptr, nullptr);
-        cudaGraphConditionalHandle h = 0;
-        if (e == cudaSuccess) {
-            *where = "conditional handle";
-            e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
-        }
-        L.cond = (unsigned long long)h;
+        *where = "conditional handle";
+        for (int c = 0; c < chunk && e == cudaSuccess; c++)
+            e = cudaGraphConditionalHandleCreate(&h[c], g, c == 0 ? 1u : 0u, cudaGraphCondAssignDefault);
     }
+    uint32_t *words = L0.cond_flag;
     for (int c = 0; c < chunk && e == cudaSuccess; c++) {
+        // the sweeps of iteration c open slot c + 1 (none after the last)
+        Launch Lc = L;
+        if (cond) {
+            Lc.cond = c + 1 < chunk ? (unsigned long long)h[c + 1] : 0ull;
+            Lc.cond_flag = words + (c + 1);
+        }
         for (Step s : steps) {
             if (!(cond && is_replace(s))) {
-                launch(s, L, st);
+                launch(s, Lc, st);
                 continue;
             }
             cudaGraph_t g = nullptr;
@@ -356,7 +368,7 @@ static cudaError_t capture_attempt(cudaStream_t st, cudaStream_t side, const Lau
             cudaGraphNodeParams np{};
             memset(static_cast<void *>(&np), 0, sizeof(np));
             np.type = cudaGraphNodeTypeConditional;
-            np.conditional.handle = (cudaGraphConditionalHandle)L.cond;
+            np.conditional.handle = h[c];
             np.conditional.type = cudaGraphCondTypeIf;
             np.conditional.size = 1;
             cudaGraphNode_t node = nullptr;
@@ -367,8 +379,10 @@ static cudaError_t capture_attempt(cudaStream_t st, cudaStream_t side, const Lau
             e = cudaStreamBeginCaptureToGraph(side, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal);
             if (e != cudaSuccess) break;
-            launch(s, L, side);
-            launch_cond_reset(L, side);
+            Launch Lr = L;  // the replacement itself opens nothing
+            Lr.cond_flag = words;
+            launch(s, Lr, side);
+            launch_cond_reset(words + c, words + kMaxCondSlots + 1, side);
             cudaGraph_t body = nullptr;
             e = cudaStreamEndCapture(side, &body);
             if (e != cudaSuccess) break;
@@ -390,18 +404,20 @@ static cudaError_t capture_attempt(cudaStream_t st, cudaStream_t side, const Lau
 // Captures `chunk` iterations of `steps` on `st` into an executable graph.
 // A MIXED iteration's residual-replacement step becomes a conditional (IF)
 // node whose body is the replacement kernel and a one-thread reset kernel:
-// the sweeps open it from the device (cudaGraphSetConditional) when a
-// right-hand side asks for a replacement, so the idle slot costs no launch.
-// The condition defaults to open at every replay of the graph, so a request
-// made in the last iteration of a chunk is served at the head of the next.
-// L.cond_flag (two device words, zero) must be set for the conditional form;
+// the sweeps of the iteration before open it from the device
+// (cudaGraphSetConditional) when a right-hand side asks for a replacement,
+// so an idle slot launches nothing.  The first slot of the graph is open at
+// every replay, so a request made in the last iteration of a replay is
+// served at the head of the next.  L.cond_flag must point to
+// kCondWords zeroed device words for the conditional form;
 // FAST_TAU_COND_REPLACE=0 captures the plain launch instead, and so does a
 // driver that refuses the conditional node (the reason is printed with
 // FAST_TAU_TRACE=1).
 int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const std::vector<Step> &steps, int chunk,
                   void (*launch)(Step, const Launch &, cudaStream_t), cudaGraphExec_t *exec, bool *used_cond)
 {
-    bool cond = L0.cond_flag != nullptr && side != nullptr && env_int("FAST_TAU_COND_REPLACE", 1) != 0;
+    bool cond = L0.cond_flag != nullptr && side != nullptr && chunk <= kMaxCondSlots &&
+                env_int("FAST_TAU_COND_REPLACE", 1) != 0;
     bool any = false;
     for (Step s : steps) any |= is_replace(s);
     cond = cond && any;
@@ -425,6 +441,13 @@ int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const st
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail(FAST_CUDA_ERROR, "graph instantiate failed: %s", cudaGetErrorString(e));
     return FAST_OK;
+}
+
+uint32_t cond_bodies_run(const uint32_t *words)
+{
+    uint32_t n = 0;
+    if (cudaMemcpy(&n, words + kMaxCondSlots + 1, sizeof(n), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+    return n;
 }
 
 // Replays `chunk` iterations from a captured graph until every job has left
@@ -512,11 +535,9 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
     if (cond && cerr == cudaSuccess) {
         // conditional replacement slots that ran: the replacement kernel and
         // the slot's reset kernel each
-        uint32_t bodies = 0;
-        if (cudaMemcpy(&bodies, L.cond_flag + 1, sizeof(bodies), cudaMemcpyDeviceToHost) == cudaSuccess) {
-            t_prof.st.launches += 2ull * bodies;
-            t_prof.st.kernel_launches[FAST_K_REPLACE] += bodies;
-        }
+        const uint32_t bodies = cond_bodies_run(L.cond_flag);
+        t_prof.st.launches += 2ull * bodies;
+        t_prof.st.kernel_launches[FAST_K_REPLACE] += bodies;
     }
     cudaEventDestroy(ev[0]);
     cudaEventDestroy(ev[1]);
@@ -683,7 +704,7 @@ size_t solve_bytes(const std::vector<VolSpec> &vols, const std::vector<JobSpec> 
     for (const JobSpec &j : jobs) need += job_bytes(vols[j.vol].nx, vols[j.vol].ny, vols[j.vol].nz, prec, solver, zc);
     const size_t nj = jobs.size(), nv = vols.size();
     need += align_up(sizeof(Scalars) * nj, 256) + align_up(sizeof(uint32_t) * nj, 256) +
-            align_up(sizeof(Job) * (nj + nv), 256) + 256;  // + the replacement slot's condition words
+            align_up(sizeof(Job) * (nj + nv), 256) + align_up(kCondWords * sizeof(uint32_t), 256);
     return need;
 }
 
@@ -822,7 +843,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     Scalars *d_sc = (Scalars *)A.take(sizeof(Scalars) * nj);
     uint32_t *d_cnt = (uint32_t *)A.take(sizeof(uint32_t) * nj);
     Job *d_jobs = (Job *)A.take(sizeof(Job) * (nj + nv));  // jobs, then one code job per volume
-    uint32_t *d_cond = (uint32_t *)A.take(2 * sizeof(uint32_t));  // replacement slot: [0] elector, [1] bodies run
+    uint32_t *d_cond = (uint32_t *)A.take(kCondWords * sizeof(uint32_t));  // conditional replacement slots
     std::vector<uint8_t *> d_code(nv);
     std::vector<int> first_job(nv, -1);
     for (int v = 0; v < nv; v++) {
@@ -865,7 +886,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     CU(cudaMemcpyAsync(d_jobs, hj, sizeof(Job) * (nj + nv), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_sc, hs, sizeof(Scalars) * nj, cudaMemcpyHostToDevice, st));
     CU(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t) * nj, st));
-    CU(cudaMemsetAsync(d_cond, 0, 2 * sizeof(uint32_t), st));
+    CU(cudaMemsetAsync(d_cond, 0, kCondWords * sizeof(uint32_t), st));
     // The staging buffers are reused below: wait for the copies to land.
     CU(cudaStreamSynchronize(st));
 
