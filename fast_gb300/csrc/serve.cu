@@ -314,7 +314,12 @@ int rebuild(Ctx &C)
         if (s != FAST_OK) return s;
         std::vector<Step> steps;
         steps_of(C, g, steps);
-        const Launch L{G.d_jobs, (int32_t)jobs.size(), 0, G.nblocks, 0ull, G.d_cond};
+        const bool mixed = C.cfg.precision == FAST_PREC_MIXED;
+        // the replacement gate opens for the group's new solves (they start
+        // with a pending replacement); an extra scan for the others is cheap
+        if (mixed) SV(cudaMemsetAsync(G.d_cond + kCondWords, 1, 1, C.st));
+        const Launch L{G.d_jobs, (int32_t)jobs.size(), 0, G.nblocks, 0ull, G.d_cond,
+                       mixed ? G.d_cond + kCondWords : nullptr};
         bool cond = false;
         s = capture_chunk(C.st, C.side, L, steps, C.cfg.chunk,
                           C.cfg.precision == FAST_PREC_MIXED ? dispatch_mixed
@@ -447,12 +452,12 @@ int create(const fast_ctx_config &cfg, Ctx **out)
         cudaMallocAsync((void **)&C->d_tmp[0], sizeof(Job) * K, C->st) != cudaSuccess ||
         cudaMallocAsync((void **)&C->d_tmp[1], sizeof(Job) * K, C->st) != cudaSuccess ||
         cudaMallocAsync((void **)&C->d_tmp[2], sizeof(Job) * K, C->st) != cudaSuccess ||
-        cudaMallocAsync((void **)&C->groups[0].d_cond, kCondWords * sizeof(uint32_t), C->st) != cudaSuccess ||
-        cudaMallocAsync((void **)&C->groups[1].d_cond, kCondWords * sizeof(uint32_t), C->st) != cudaSuccess)
+        cudaMallocAsync((void **)&C->groups[0].d_cond, (kCondWords + 1) * sizeof(uint32_t), C->st) != cudaSuccess ||
+        cudaMallocAsync((void **)&C->groups[1].d_cond, (kCondWords + 1) * sizeof(uint32_t), C->st) != cudaSuccess)
         return fin(ft_fail(FAST_NOMEM, "context tables"));
     if (cudaMemsetAsync(C->d_cnt, 0, sizeof(uint32_t) * K, C->st) != cudaSuccess ||
-        cudaMemsetAsync(C->groups[0].d_cond, 0, kCondWords * sizeof(uint32_t), C->st) != cudaSuccess ||
-        cudaMemsetAsync(C->groups[1].d_cond, 0, kCondWords * sizeof(uint32_t), C->st) != cudaSuccess ||
+        cudaMemsetAsync(C->groups[0].d_cond, 0, (kCondWords + 1) * sizeof(uint32_t), C->st) != cudaSuccess ||
+        cudaMemsetAsync(C->groups[1].d_cond, 0, (kCondWords + 1) * sizeof(uint32_t), C->st) != cudaSuccess ||
         cudaMallocHost(&C->h_snap[0], sizeof(Scalars) * K) != cudaSuccess ||
         cudaMallocHost(&C->h_snap[1], sizeof(Scalars) * K) != cudaSuccess ||
         cudaMallocHost(&C->h_init, sizeof(Scalars) * K) != cudaSuccess ||

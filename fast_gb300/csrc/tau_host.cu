@@ -417,7 +417,7 @@ int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const st
                   void (*launch)(Step, const Launch &, cudaStream_t), cudaGraphExec_t *exec, bool *used_cond)
 {
     bool cond = L0.cond_flag != nullptr && side != nullptr && chunk <= kMaxCondSlots &&
-                env_int("FAST_TAU_COND_REPLACE", 1) != 0;
+                env_int("FAST_TAU_COND_REPLACE", 0) != 0;
     bool any = false;
     for (Step s : steps) any |= is_replace(s);
     cond = cond && any;
@@ -704,7 +704,7 @@ size_t solve_bytes(const std::vector<VolSpec> &vols, const std::vector<JobSpec> 
     for (const JobSpec &j : jobs) need += job_bytes(vols[j.vol].nx, vols[j.vol].ny, vols[j.vol].nz, prec, solver, zc);
     const size_t nj = jobs.size(), nv = vols.size();
     need += align_up(sizeof(Scalars) * nj, 256) + align_up(sizeof(uint32_t) * nj, 256) +
-            align_up(sizeof(Job) * (nj + nv), 256) + align_up(kCondWords * sizeof(uint32_t), 256);
+            align_up(sizeof(Job) * (nj + nv), 256) + align_up((kCondWords + 1) * sizeof(uint32_t), 256);
     return need;
 }
 
@@ -843,7 +843,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     Scalars *d_sc = (Scalars *)A.take(sizeof(Scalars) * nj);
     uint32_t *d_cnt = (uint32_t *)A.take(sizeof(uint32_t) * nj);
     Job *d_jobs = (Job *)A.take(sizeof(Job) * (nj + nv));  // jobs, then one code job per volume
-    uint32_t *d_cond = (uint32_t *)A.take(kCondWords * sizeof(uint32_t));  // conditional replacement slots
+    uint32_t *d_cond = (uint32_t *)A.take((kCondWords + 1) * sizeof(uint32_t));  // replacement gate + conditional slots
     std::vector<uint8_t *> d_code(nv);
     std::vector<int> first_job(nv, -1);
     for (int v = 0; v < nv; v++) {
@@ -886,12 +886,15 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     CU(cudaMemcpyAsync(d_jobs, hj, sizeof(Job) * (nj + nv), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_sc, hs, sizeof(Scalars) * nj, cudaMemcpyHostToDevice, st));
     CU(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t) * nj, st));
-    CU(cudaMemsetAsync(d_cond, 0, kCondWords * sizeof(uint32_t), st));
+    CU(cudaMemsetAsync(d_cond, 0, (kCondWords + 1) * sizeof(uint32_t), st));
+    // every MIXED right-hand side starts with a pending replacement (x = x0):
+    // the gate word reads 1
+    if (mixed) CU(cudaMemsetAsync(d_cond + kCondWords, 1, 1, st));
     // The staging buffers are reused below: wait for the copies to land.
     CU(cudaStreamSynchronize(st));
 
-    Launch L{d_jobs, nj, 0, tile_base, 0ull, d_cond};
-    Launch LC{d_jobs + nj, nv, 0, code_base, 0ull, nullptr};
+    Launch L{d_jobs, nj, 0, tile_base, 0ull, d_cond, mixed ? d_cond + kCondWords : nullptr};
+    Launch LC{d_jobs + nj, nv, 0, code_base, 0ull, nullptr, nullptr};
 
     int status = FAST_OK;
     launch_counted(FAST_K_CODE, st, [&] { launch_code(LC, st); });

@@ -249,6 +249,17 @@ struct RedType<Op, std::void_t<typename Op::R>> {
     using type = typename Op::R;
 };
 
+// Operations that run first after the MIXED replacement slot clear the
+// launch's gate word (Op::clears_gate).
+template <class Op, class = void>
+struct GateRole {
+    static constexpr bool clears = false;
+};
+template <class Op>
+struct GateRole<Op, std::void_t<decltype(Op::clears_gate)>> {
+    static constexpr bool clears = Op::clears_gate;
+};
+
 // The sweep of one tile `blk` (a block index of the launch), shared by the
 // kernel entries below.  `qb` counts the planes this block has taken through
 // its stage ring so far (ring slot and mbarrier phase continue from it), and
@@ -275,6 +286,9 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
     __shared__ typename Op::Shared S;
 
     const int tid = threadIdx.x;
+    // The first sweep after the replacement slot re-arms the launch's gate
+    // (before any block of it can arrive at the finisher, which may set it).
+    if (GateRole<Op>::clears && L.gate != nullptr && blk == 0 && tid == 0) *L.gate = 0u;
     __syncthreads();  // the previous tile of this block is done with the shared state
     if (tid == 0) {
         s_job = find_job(L, blk);
@@ -473,6 +487,7 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
             for (int k = 0; k < NV && k < 4; k++) J.sc->dbg[k] = tot[k];
             Op::finish(*J.sc, tot);
             *J.counter = 0u;
+            if (L.gate != nullptr && J.sc->replace != 0 && J.sc->state == RUNNING) *L.gate = 1u;
             // A MIXED right-hand side that now asks for a residual
             // replacement opens the conditional replacement slot of the
             // captured iteration; one setter per epoch (the slot's reset
@@ -513,6 +528,9 @@ __global__ void __launch_bounds__(NTHREADS, MB) sweep_kernel_mb(Launch L)
 template <class Op, int NSTAGE>
 __global__ void __launch_bounds__(NTHREADS) sweep_kernel_tiles(Launch L)
 {
+    // No replacement pending in the whole launch: leave without touching
+    // the job table.
+    if (L.gate != nullptr && __ldcg(L.gate) == 0u) return;
     int qb = 0;
     bool ready = false;
     for (int64_t blk = blockIdx.x; blk < L.nblocks;) {
@@ -726,6 +744,7 @@ template <typename TT, typename ST>
 struct OpCG1 {
     using T = TT;
     static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
+    static constexpr bool clears_gate = FB;
     static constexpr uint32_t wait_hint_ns = FB ? FAST_TAU_HINT_CG : 0;
     using SL = Streams<sizeof(TT), sizeof(TT), 1>;
     static constexpr int NV = 1;
@@ -1290,6 +1309,7 @@ __device__ __forceinline__ void bicg2_k2_finish(Scalars &sc, double ts, double t
 struct OpBiK1 {
     using T = float;
     static constexpr bool FB = true;
+    static constexpr bool clears_gate = true;
     static constexpr uint32_t wait_hint_ns = FAST_TAU_HINT_K1;
     using SL = Streams<4, 4, 4, 4, 4, 4, 1>;  // r, v, t, p, e, r0, code
     static constexpr int NV = 2;
@@ -1505,6 +1525,7 @@ __device__ __forceinline__ void cgf_finish(Scalars &sc, double gamma, double del
 struct OpCGF {
     using T = float;
     static constexpr bool FB = true;
+    static constexpr bool clears_gate = true;
     static constexpr uint32_t wait_hint_ns = FAST_TAU_HINT_CGF;
     using SL = Streams<4, 4, 4, 4, 4, 1>;  // r, s, w, p, e, code
     static constexpr int NV = 3;

@@ -142,6 +142,11 @@ struct Launch {
     // every iteration) and a device word that elects one setter per epoch.
     unsigned long long cond;
     uint32_t *cond_flag;
+    // MIXED: one device word, nonzero while a residual replacement is
+    // pending for some right-hand side of the launch (null otherwise).  The
+    // replacement kernel's blocks leave at once while it is zero; the first
+    // sweep after the slot clears it and any sweep that asks sets it.
+    uint32_t *gate;
 };
 
 }  // namespace ft
