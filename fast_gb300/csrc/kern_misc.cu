@@ -57,19 +57,6 @@ cudaError_t configure_misc()
     return cudaSuccess;
 }
 
-// The last node of a conditional replacement slot: re-arm the slot's
-// election word for the next replay and count the slot bodies that ran.
-__global__ void cond_reset_kernel(uint32_t *elector, uint32_t *count)
-{
-    *elector = 0u;
-    *count += 1u;
-}
-
-void launch_cond_reset(uint32_t *elector, uint32_t *count, cudaStream_t st)
-{
-    cond_reset_kernel<<<1, 1, 0, st>>>(elector, count);
-}
-
 void launch_init64(const Launch &L, cudaStream_t st) { init64_kernel<<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L); }
 
 void launch_code(const Launch &L, cudaStream_t st) { code_kernel<<<(unsigned)L.nblocks, NTHREADS, 0, st>>>(L); }

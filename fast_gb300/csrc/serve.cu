@@ -73,14 +73,13 @@ struct Group {
     Job *d_jobs = nullptr;          // device job table (capacity kMax)
     cudaGraphExec_t exec = nullptr;
     int64_t nblocks = 0;
-    uint32_t *d_cond = nullptr;     // the chunk graph's replacement-slot words (MIXED)
+    uint32_t *d_gate = nullptr;     // the group's replacement gate word (MIXED)
 };
 
 struct Ctx {
     fast_ctx_config cfg;
     fast_tau_params P[2];  // by solver
     cudaStream_t st = nullptr;
-    cudaStream_t side = nullptr;   // captures conditional-node bodies
     Clock::time_point t0;
     int kMax = 0;
     Scalars *d_slots = nullptr;
@@ -317,14 +316,12 @@ int rebuild(Ctx &C)
         const bool mixed = C.cfg.precision == FAST_PREC_MIXED;
         // the replacement gate opens for the group's new solves (they start
         // with a pending replacement); an extra scan for the others is cheap
-        if (mixed) SV(cudaMemsetAsync(G.d_cond + kCondWords, 1, 1, C.st));
-        const Launch L{G.d_jobs, (int32_t)jobs.size(), 0, G.nblocks, 0ull, G.d_cond,
-                       mixed ? G.d_cond + kCondWords : nullptr};
-        bool cond = false;
-        s = capture_chunk(C.st, C.side, L, steps, C.cfg.chunk,
+        if (mixed) SV(cudaMemsetAsync(G.d_gate, 1, 1, C.st));
+        const Launch L{G.d_jobs, (int32_t)jobs.size(), 0, G.nblocks, mixed ? G.d_gate : nullptr};
+        s = capture_chunk(C.st, L, steps, C.cfg.chunk,
                           C.cfg.precision == FAST_PREC_MIXED ? dispatch_mixed
                           : C.cfg.precision == FAST_PREC_F64 ? launch_pure_f64 : launch_pure_f32,
-                          &G.exec, &cond);
+                          &G.exec);
         if (s != FAST_OK) return s;
     }
     C.dirty = false;
@@ -391,7 +388,7 @@ void destroy(Ctx *C)
     for (Group &G : C->groups) {
         if (G.exec) cudaGraphExecDestroy(G.exec);
         if (G.d_jobs) cudaFreeAsync(G.d_jobs, C->st);
-        if (G.d_cond) cudaFreeAsync(G.d_cond, C->st);
+        if (G.d_gate) cudaFreeAsync(G.d_gate, C->st);
     }
     for (Job *d : C->d_tmp)
         if (d) cudaFreeAsync(d, C->st);
@@ -406,7 +403,6 @@ void destroy(Ctx *C)
         if (e) cudaEventDestroy(e);
     if (C->ev_copy) cudaEventDestroy(C->ev_copy);
     if (C->st) cudaStreamDestroy(C->st);
-    if (C->side) cudaStreamDestroy(C->side);
     delete C;
 }
 
@@ -440,7 +436,6 @@ int create(const fast_ctx_config &cfg, Ctx **out)
         return st;
     };
     if (cudaStreamCreateWithFlags(&C->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&C->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&C->ev[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&C->ev[1], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&C->ev_copy, cudaEventDisableTiming) != cudaSuccess)
@@ -452,12 +447,12 @@ int create(const fast_ctx_config &cfg, Ctx **out)
         cudaMallocAsync((void **)&C->d_tmp[0], sizeof(Job) * K, C->st) != cudaSuccess ||
         cudaMallocAsync((void **)&C->d_tmp[1], sizeof(Job) * K, C->st) != cudaSuccess ||
         cudaMallocAsync((void **)&C->d_tmp[2], sizeof(Job) * K, C->st) != cudaSuccess ||
-        cudaMallocAsync((void **)&C->groups[0].d_cond, (kCondWords + 1) * sizeof(uint32_t), C->st) != cudaSuccess ||
-        cudaMallocAsync((void **)&C->groups[1].d_cond, (kCondWords + 1) * sizeof(uint32_t), C->st) != cudaSuccess)
+        cudaMallocAsync((void **)&C->groups[0].d_gate, sizeof(uint32_t), C->st) != cudaSuccess ||
+        cudaMallocAsync((void **)&C->groups[1].d_gate, sizeof(uint32_t), C->st) != cudaSuccess)
         return fin(ft_fail(FAST_NOMEM, "context tables"));
     if (cudaMemsetAsync(C->d_cnt, 0, sizeof(uint32_t) * K, C->st) != cudaSuccess ||
-        cudaMemsetAsync(C->groups[0].d_cond, 0, (kCondWords + 1) * sizeof(uint32_t), C->st) != cudaSuccess ||
-        cudaMemsetAsync(C->groups[1].d_cond, 0, (kCondWords + 1) * sizeof(uint32_t), C->st) != cudaSuccess ||
+        cudaMemsetAsync(C->groups[0].d_gate, 0, sizeof(uint32_t), C->st) != cudaSuccess ||
+        cudaMemsetAsync(C->groups[1].d_gate, 0, sizeof(uint32_t), C->st) != cudaSuccess ||
         cudaMallocHost(&C->h_snap[0], sizeof(Scalars) * K) != cudaSuccess ||
         cudaMallocHost(&C->h_snap[1], sizeof(Scalars) * K) != cudaSuccess ||
         cudaMallocHost(&C->h_init, sizeof(Scalars) * K) != cudaSuccess ||

@@ -19,7 +19,6 @@ namespace ft {
 struct Engine {
     int device = -1;
     cudaStream_t stream = nullptr;
-    cudaStream_t side = nullptr;   // captures the bodies of conditional graph nodes
     Scalars *h_sc = nullptr;   // pinned, 2 * kMaxJobs (double-buffered poll)
     Job *h_jobs = nullptr;     // pinned staging for job descriptors (2 * kMaxJobs)
     static constexpr int kMaxJobs = 1024;
@@ -79,15 +78,9 @@ void dispatch_mixed(Step s, const Launch &L, cudaStream_t st);
 // The per-iteration steps of a MIXED solve (CG: one fused sweep, or the
 // classic two with FAST_TAU_CG_FUSED=0).
 bool cg_fused_enabled();
-bool is_replace(Step s);
-// Device words of a chunk graph's conditional replacement slots (election
-// words of up to 63 slots, then the count of slot bodies that ran).
-constexpr int kCondWords = 64 + 1;
-uint32_t cond_bodies_run(const uint32_t *words);
-// Captures `chunk` iterations of `steps` into an executable graph, the MIXED
-// replacement slot as a conditional node when L.cond_flag is set.
-int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L, const std::vector<Step> &steps, int chunk,
-                  void (*launch)(Step, const Launch &, cudaStream_t), cudaGraphExec_t *exec, bool *used_cond);
+// Captures `chunk` iterations of `steps` on `st` into an executable graph.
+int capture_chunk(cudaStream_t st, const Launch &L, const std::vector<Step> &steps, int chunk,
+                  void (*launch)(Step, const Launch &, cudaStream_t), cudaGraphExec_t *exec);
 // MIXED steps of one iteration: the replacement slot (FP64 iterate, or
 // float-float with `ff`) and the FP32 sweeps.
 std::vector<Step> mixed_steps(int solver, bool ff);

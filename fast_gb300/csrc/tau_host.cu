@@ -90,7 +90,6 @@ int Engine::init(int dev)
     device = dev;
     CU(cudaSetDevice(dev));
     CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    CU(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     CU(cudaMallocHost(&h_sc, sizeof(Scalars) * 2 * kMaxJobs));
     CU(cudaMallocHost(&h_jobs, sizeof(Job) * 2 * kMaxJobs));  // jobs + one code job per volume
     cudaError_t ce = configure_f64();
@@ -304,150 +303,20 @@ int tensor_map(CUtensorMap *tm, const void *base, int es, int64_t nx, int64_t ny
     return FAST_OK;
 }
 
-bool is_replace(Step s)
-{
-    return s == Step::REPLACE_CG || s == Step::REPLACE_BI || s == Step::REPLACE_CG_FF || s == Step::REPLACE_BI_FF;
-}
-
 // Captures `chunk` iterations of `steps` on `st` into an executable graph.
-// A MIXED iteration's residual-replacement step becomes a conditional (IF)
-// node whose body is the replacement kernel and a one-thread reset kernel:
-// the sweeps open it from the device (cudaGraphSetConditional) when a
-// right-hand side asks for a replacement, so the idle slot costs no launch.
-// The condition defaults to open at every replay of the graph, so a request
-// made in the last iteration of a chunk is served at the head of the next.
-// L.cond_flag (two device words, zero) must be set for the conditional form;
-// FAST_TAU_COND_REPLACE=0 captures the plain launch instead.
-// Words of a chunk graph's conditional replacement slots: one election word
-// per slot, then the count of slot bodies that ran.
-constexpr int kMaxCondSlots = 63;
-
-static cudaError_t capture_attempt(cudaStream_t st, cudaStream_t side, const Launch &L0, const std::vector<Step> &steps,
-                                   int chunk, void (*launch)(Step, const Launch &, cudaStream_t), bool cond,
-                                   cudaGraph_t *graph, const char **where)
+int capture_chunk(cudaStream_t st, const Launch &L, const std::vector<Step> &steps, int chunk,
+                  void (*launch)(Step, const Launch &, cudaStream_t), cudaGraphExec_t *exec)
 {
-    Launch L = L0;
-    L.cond = 0ull;
-    *graph = nullptr;
-    *where = "begin capture";
-    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
-    cudaStreamCaptureStatus cst;
-    // One handle per slot (a handle belongs to one conditional node): slot 0
-    // defaults to open at every replay (it serves requests made in the last
-    // iteration of the previous replay), the others to closed.
-    std::vector<cudaGraphConditionalHandle> h(cond ? chunk : 0, 0);
-    if (cond) {
-        cudaGraph_t g = nullptr;
-        *where = "capture info";
-        e = cudaStreamGetCaptureInfo(st, &cst, nullptr, &g, nullptr, nullptr, nullptr);
-        *where = "conditional handle";
-        for (int c = 0; c < chunk && e == cudaSuccess; c++)
-            e = cudaGraphConditionalHandleCreate(&h[c], g, c == 0 ? 1u : 0u, cudaGraphCondAssignDefault);
-    }
-    uint32_t *words = L0.cond_flag;
-    for (int c = 0; c < chunk && e == cudaSuccess; c++) {
-        // the sweeps of iteration c open slot c + 1 (none after the last)
-        Launch Lc = L;
-        if (cond) {
-            Lc.cond = c + 1 < chunk ? (unsigned long long)h[c + 1] : 0ull;
-            Lc.cond_flag = words + (c + 1);
-        }
-        for (Step s : steps) {
-            if (!(cond && is_replace(s))) {
-                launch(s, Lc, st);
-                continue;
-            }
-            cudaGraph_t g = nullptr;
-            const cudaGraphNode_t *deps = nullptr;
-            const cudaGraphEdgeData *edges = nullptr;
-            size_t ndeps = 0;
-            *where = "capture dependencies";
-            e = cudaStreamGetCaptureInfo(st, &cst, nullptr, &g, &deps, &edges, &ndeps);
-            if (e != cudaSuccess) break;
-            cudaGraphNodeParams np{};
-            memset(static_cast<void *>(&np), 0, sizeof(np));
-            np.type = cudaGraphNodeTypeConditional;
-            np.conditional.handle = h[c];
-            np.conditional.type = cudaGraphCondTypeIf;
-            np.conditional.size = 1;
-            cudaGraphNode_t node = nullptr;
-            *where = "conditional node";
-            e = cudaGraphAddNode(&node, g, deps, edges, ndeps, &np);
-            if (e != cudaSuccess) break;
-            *where = "capture of the conditional body";
-            e = cudaStreamBeginCaptureToGraph(side, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                              cudaStreamCaptureModeThreadLocal);
-            if (e != cudaSuccess) break;
-            Launch Lr = L;  // the replacement itself opens nothing
-            Lr.cond_flag = words;
-            launch(s, Lr, side);
-            launch_cond_reset(words + c, words + kMaxCondSlots + 1, side);
-            cudaGraph_t body = nullptr;
-            e = cudaStreamEndCapture(side, &body);
-            if (e != cudaSuccess) break;
-            *where = "capture dependency update";
-            e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-            if (e != cudaSuccess) break;
-        }
-    }
-    cudaError_t ee = cudaStreamEndCapture(st, graph);
-    if (e == cudaSuccess && ee != cudaSuccess) *where = "end capture";
-    if (e == cudaSuccess) e = ee;
-    if (e != cudaSuccess && *graph) {
-        cudaGraphDestroy(*graph);
-        *graph = nullptr;
-    }
-    return e;
-}
-
-// Captures `chunk` iterations of `steps` on `st` into an executable graph.
-// A MIXED iteration's residual-replacement step becomes a conditional (IF)
-// node whose body is the replacement kernel and a one-thread reset kernel:
-// the sweeps of the iteration before open it from the device
-// (cudaGraphSetConditional) when a right-hand side asks for a replacement,
-// so an idle slot launches nothing.  The first slot of the graph is open at
-// every replay, so a request made in the last iteration of a replay is
-// served at the head of the next.  L.cond_flag must point to
-// kCondWords zeroed device words for the conditional form;
-// FAST_TAU_COND_REPLACE=0 captures the plain launch instead, and so does a
-// driver that refuses the conditional node (the reason is printed with
-// FAST_TAU_TRACE=1).
-int capture_chunk(cudaStream_t st, cudaStream_t side, const Launch &L0, const std::vector<Step> &steps, int chunk,
-                  void (*launch)(Step, const Launch &, cudaStream_t), cudaGraphExec_t *exec, bool *used_cond)
-{
-    bool cond = L0.cond_flag != nullptr && side != nullptr && chunk <= kMaxCondSlots &&
-                env_int("FAST_TAU_COND_REPLACE", 0) != 0;
-    bool any = false;
-    for (Step s : steps) any |= is_replace(s);
-    cond = cond && any;
     cudaGraph_t graph = nullptr;
-    const char *where = "";
-    cudaError_t e = capture_attempt(st, side, L0, steps, chunk, launch, cond, &graph, &where);
-    if (e != cudaSuccess && cond) {
-        if (env_int("FAST_TAU_TRACE", 0))
-            fprintf(stderr, "fasttau: conditional replacement slot not captured (%s: %s); plain slot used\n", where,
-                    cudaGetErrorString(e));
-        cudaGetLastError();
-        cond = false;
-        e = capture_attempt(st, side, L0, steps, chunk, launch, false, &graph, &where);
-    }
-    *used_cond = cond;
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(FAST_CUDA_ERROR, "graph capture failed (%s): %s", where, cudaGetErrorString(e));
-    }
+    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int c = 0; c < chunk; c++)
+        for (Step s : steps) launch(s, L, st);
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) return fail(FAST_CUDA_ERROR, "graph capture failed: %s", cudaGetErrorString(e));
     e = cudaGraphInstantiate(exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail(FAST_CUDA_ERROR, "graph instantiate failed: %s", cudaGetErrorString(e));
     return FAST_OK;
-}
-
-uint32_t cond_bodies_run(const uint32_t *words)
-{
-    uint32_t n = 0;
-    if (cudaMemcpy(&n, words + kMaxCondSlots + 1, sizeof(n), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
-    return n;
 }
 
 // Replays `chunk` iterations from a captured graph until every job has left
@@ -499,8 +368,7 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
         return FAST_OK;
     }
     cudaGraphExec_t exec = nullptr;
-    bool cond = false;
-    int cs = capture_chunk(st, E.side, L, steps, chunk, launch, &exec, &cond);
+    int cs = capture_chunk(st, L, steps, chunk, launch, &exec);
     if (cs != FAST_OK) return cs;
     cudaError_t cerr = cudaSuccess;
 
@@ -514,11 +382,8 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
         cerr = cudaGraphLaunch(exec, st);
         if (cerr != cudaSuccess) { status = fail(FAST_CUDA_ERROR, "graph launch: %s", cudaGetErrorString(cerr)); break; }
         t_prof.st.graph_replays += 1;
-        for (Step s : steps) {
-            if (cond && is_replace(s)) continue;  // counted from the device below
-            t_prof.st.launches += (uint64_t)chunk;
-            t_prof.st.kernel_launches[kind_of(s)] += (uint64_t)chunk;
-        }
+        t_prof.st.launches += (uint64_t)chunk * steps.size();
+        for (Step s : steps) t_prof.st.kernel_launches[kind_of(s)] += (uint64_t)chunk;
         Scalars *hb = E.h_sc + (k & 1) * Engine::kMaxJobs;
         cudaMemcpyAsync(hb, d_sc, sizeof(Scalars) * njobs, cudaMemcpyDeviceToHost, st);
         cudaEventRecord(ev[k & 1], st);
@@ -532,13 +397,6 @@ int iterate(Engine &E, const Launch &L, int njobs, Scalars *d_sc, const std::vec
     }
     cerr = cudaStreamSynchronize(st);
     if (cerr != cudaSuccess && status == FAST_OK) status = fail(FAST_CUDA_ERROR, "solver: %s", cudaGetErrorString(cerr));
-    if (cond && cerr == cudaSuccess) {
-        // conditional replacement slots that ran: the replacement kernel and
-        // the slot's reset kernel each
-        const uint32_t bodies = cond_bodies_run(L.cond_flag);
-        t_prof.st.launches += 2ull * bodies;
-        t_prof.st.kernel_launches[FAST_K_REPLACE] += bodies;
-    }
     cudaEventDestroy(ev[0]);
     cudaEventDestroy(ev[1]);
     cudaGraphExecDestroy(exec);
@@ -704,7 +562,7 @@ size_t solve_bytes(const std::vector<VolSpec> &vols, const std::vector<JobSpec> 
     for (const JobSpec &j : jobs) need += job_bytes(vols[j.vol].nx, vols[j.vol].ny, vols[j.vol].nz, prec, solver, zc);
     const size_t nj = jobs.size(), nv = vols.size();
     need += align_up(sizeof(Scalars) * nj, 256) + align_up(sizeof(uint32_t) * nj, 256) +
-            align_up(sizeof(Job) * (nj + nv), 256) + align_up((kCondWords + 1) * sizeof(uint32_t), 256);
+            align_up(sizeof(Job) * (nj + nv), 256) + 256;  // + the replacement gate word
     return need;
 }
 
@@ -843,7 +701,7 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     Scalars *d_sc = (Scalars *)A.take(sizeof(Scalars) * nj);
     uint32_t *d_cnt = (uint32_t *)A.take(sizeof(uint32_t) * nj);
     Job *d_jobs = (Job *)A.take(sizeof(Job) * (nj + nv));  // jobs, then one code job per volume
-    uint32_t *d_cond = (uint32_t *)A.take((kCondWords + 1) * sizeof(uint32_t));  // replacement gate + conditional slots
+    uint32_t *d_gate = (uint32_t *)A.take(sizeof(uint32_t));  // MIXED replacement gate
     std::vector<uint8_t *> d_code(nv);
     std::vector<int> first_job(nv, -1);
     for (int v = 0; v < nv; v++) {
@@ -886,15 +744,15 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     CU(cudaMemcpyAsync(d_jobs, hj, sizeof(Job) * (nj + nv), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_sc, hs, sizeof(Scalars) * nj, cudaMemcpyHostToDevice, st));
     CU(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t) * nj, st));
-    CU(cudaMemsetAsync(d_cond, 0, (kCondWords + 1) * sizeof(uint32_t), st));
     // every MIXED right-hand side starts with a pending replacement (x = x0):
     // the gate word reads 1
-    if (mixed) CU(cudaMemsetAsync(d_cond + kCondWords, 1, 1, st));
+    CU(cudaMemsetAsync(d_gate, 0, sizeof(uint32_t), st));
+    if (mixed) CU(cudaMemsetAsync(d_gate, 1, 1, st));
     // The staging buffers are reused below: wait for the copies to land.
     CU(cudaStreamSynchronize(st));
 
-    Launch L{d_jobs, nj, 0, tile_base, 0ull, d_cond, mixed ? d_cond + kCondWords : nullptr};
-    Launch LC{d_jobs + nj, nv, 0, code_base, 0ull, nullptr, nullptr};
+    Launch L{d_jobs, nj, 0, tile_base, mixed ? d_gate : nullptr};
+    Launch LC{d_jobs + nj, nv, 0, code_base, nullptr};
 
     int status = FAST_OK;
     launch_counted(FAST_K_CODE, st, [&] { launch_code(LC, st); });

@@ -22,9 +22,6 @@ void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st);
 // asked for one): FP64 iterate, or float-float with `ff`.
 void launch_replace(bool bicg, bool ff, const Launch &L, cudaStream_t st);
 void launch_init64(const Launch &L, cudaStream_t st);
-// Last node of a conditional replacement slot: re-arms its election word and
-// counts the slot bodies that ran.
-void launch_cond_reset(uint32_t *elector, uint32_t *count, cudaStream_t st);
 void launch_code(const Launch &L, cudaStream_t st);
 // tau flux sum: src 0 = double x, 1 = float x, 2 = the current MIXED iterate
 // as float-float pairs, 3 = the current MIXED iterate as doubles.

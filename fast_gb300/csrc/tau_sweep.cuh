@@ -488,13 +488,6 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
             Op::finish(*J.sc, tot);
             *J.counter = 0u;
             if (L.gate != nullptr && J.sc->replace != 0 && J.sc->state == RUNNING) *L.gate = 1u;
-            // A MIXED right-hand side that now asks for a residual
-            // replacement opens the conditional replacement slot of the
-            // captured iteration; one setter per epoch (the slot's reset
-            // kernel closes it again).
-            if (L.cond != 0ull && J.sc->replace != 0 && J.sc->state == RUNNING &&
-                atomicExch(L.cond_flag, 1u) == 0u)
-                cudaGraphSetConditional((cudaGraphConditionalHandle)L.cond, 1u);
         }
     }
     return SWEEP_DONE;

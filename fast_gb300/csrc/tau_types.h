@@ -137,11 +137,6 @@ struct Launch {
     int32_t njobs;
     int32_t pad;
     int64_t nblocks;    // total blocks = sum of job tiles
-    // Captured MIXED iterations: the graph's conditional handle of the
-    // residual-replacement slot (0: no conditional; the slot is launched
-    // every iteration) and a device word that elects one setter per epoch.
-    unsigned long long cond;
-    uint32_t *cond_flag;
     // MIXED: one device word, nonzero while a residual replacement is
     // pending for some right-hand side of the launch (null otherwise).  The
     // replacement kernel's blocks leave at once while it is zero; the first
