@@ -275,7 +275,8 @@ int64_t row_pitch(int64_t nx) { return (nx + 15) / 16 * 16; }
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::mutex g_encode_mu;
 
-int tensor_map(CUtensorMap *tm, const void *base, int es, int64_t nx, int64_t ny, int64_t nz, int64_t pitch)
+int tensor_map(CUtensorMap *tm, const void *base, int es, int64_t nx, int64_t ny, int64_t nz, int64_t pitch,
+               bool interior = false)
 {
     {
         std::lock_guard<std::mutex> lk(g_encode_mu);
@@ -293,8 +294,9 @@ int tensor_map(CUtensorMap *tm, const void *base, int es, int64_t nx, int64_t ny
     const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
     const cuuint64_t strides[2] = {(cuuint64_t)(pitch * es), (cuuint64_t)(pitch * ny * es)};
     // Box: the TX x TY tile plus a one-voxel halo, widened in x so that its
-    // start (x0 - 16/es) and width are multiples of 16 bytes.
-    const cuuint32_t box[3] = {(cuuint32_t)(TX + 2 * (16 / es)), (cuuint32_t)HY, 1u};
+    // start (x0 - 16/es) and width are multiples of 16 bytes; or (interior)
+    // the tile alone, for streams read only at a block's own points.
+    const cuuint32_t box[3] = {(cuuint32_t)(interior ? TX : TX + 2 * (16 / es)), (cuuint32_t)(interior ? TY : HY), 1u};
     const cuuint32_t estr[3] = {1u, 1u, 1u};
     CUresult r = g_encode(tm, dt, 3, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -611,9 +613,12 @@ int build_job(Job &J, Scalars &S, const uint8_t *d_mask, int64_t nx, int64_t ny,
     if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R], J.r[0], es, nx, ny, nz, pitch);
     if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P], J.p[0], es, nx, ny, nz, pitch);
     if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_P + 1], J.p[1], es, nx, ny, nz, pitch);
+    if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_XI], J.x, es, nx, ny, nz, pitch, true);
+    if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_RI], J.r[0], es, nx, ny, nz, pitch, true);
     if (ts == FAST_OK && (solver == FAST_SOLVER_BICGSTAB || fused)) {
         ts = tensor_map(&J.tm[TM_R + 1], J.r[1], es, nx, ny, nz, pitch);
         if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R0], J.r0, es, nx, ny, nz, pitch);
+        if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_R0I], J.r0, es, nx, ny, nz, pitch, true);
         if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_V], J.v[0], es, nx, ny, nz, pitch);
         if (ts == FAST_OK) ts = tensor_map(&J.tm[TM_V + 1], J.v[1], es, nx, ny, nz, pitch);
     }

@@ -140,25 +140,32 @@ __host__ __device__ constexpr int box_w(int es) { return TX + 2 * box_off(es); }
 __host__ __device__ constexpr int box_bytes(int es) { return box_w(es) * HY * es; }
 __host__ __device__ constexpr int box_alloc(int es) { return (box_bytes(es) + 127) / 128 * 128; }
 
+// A stream is named by its element size; a negative size marks a stream the
+// operation reads only at its own points (never at the halo): it is loaded
+// as the TX x TY tile alone (its tensor map has that box), which saves the
+// halo's shared memory and L2 reads.
 template <int... ES>
 struct Streams {
     static constexpr int N = sizeof...(ES);
-    __host__ __device__ static constexpr int esz(int s)
+    __host__ __device__ static constexpr int raw(int s)
     {
         constexpr int a[N] = {ES...};
         return a[s];
     }
+    __host__ __device__ static constexpr int esz(int s) { return raw(s) < 0 ? -raw(s) : raw(s); }
+    __host__ __device__ static constexpr bool interior(int s) { return raw(s) < 0; }
+    __host__ __device__ static constexpr int bytes(int s) { return interior(s) ? TX * TY * esz(s) : box_bytes(esz(s)); }
     __host__ __device__ static constexpr int off(int s)
     {
         int o = 0;
-        for (int t = 0; t < s; ++t) o += box_alloc(esz(t));
+        for (int t = 0; t < s; ++t) o += (bytes(t) + 127) / 128 * 128;
         return o;
     }
     __host__ __device__ static constexpr int stage_bytes() { return off(N); }
     __host__ __device__ static constexpr int tx_bytes()
     {
         int b = 0;
-        for (int t = 0; t < N; ++t) b += box_bytes(esz(t));
+        for (int t = 0; t < N; ++t) b += bytes(t);
         return b;
     }
 };
@@ -173,7 +180,11 @@ template <typename E, class SL, int S>
 __device__ __forceinline__ const E *sp(const unsigned char *stage, const Pt &p)
 {
     constexpr int es = (int)sizeof(E);
-    return reinterpret_cast<const E *>(stage + SL::off(S)) + p.row * box_w(es) + p.xr + box_off(es);
+    static_assert(SL::esz(S) == es, "stream element size");
+    if constexpr (SL::interior(S))  // own points only: tile rows 1..TY, x 0..TX-1
+        return reinterpret_cast<const E *>(stage + SL::off(S)) + (p.row - 1) * TX + p.xr;
+    else
+        return reinterpret_cast<const E *>(stage + SL::off(S)) + p.row * box_w(es) + p.xr + box_off(es);
 }
 
 // Element of stream S at point p.
@@ -247,6 +258,27 @@ struct RedType {
 template <class Op>
 struct RedType<Op, std::void_t<typename Op::R>> {
     using type = typename Op::R;
+};
+
+// FAST_TAU_INTERIOR=0 loads every stream with its halo (the interior-only
+// boxes off).
+#ifndef FAST_TAU_INTERIOR
+#define FAST_TAU_INTERIOR 1
+#endif
+__host__ __device__ constexpr int own_only(int es) { return FAST_TAU_INTERIOR ? -es : es; }
+
+// A lane pair of halo points: Op::load2h when the operation has streams it
+// reads only at its own points (they are not in the stage at the halo),
+// else Op::load2.
+template <class Op, class = void>
+struct HaloLoad {
+    template <class V>
+    __device__ static void pair(const unsigned char *st, const Pt &p, V &a, V &b) { Op::load2(st, p, a, b); }
+};
+template <class Op>
+struct HaloLoad<Op, std::void_t<decltype(&Op::load2h)>> {
+    template <class V>
+    __device__ static void pair(const unsigned char *st, const Pt &p, V &a, V &b) { Op::load2h(st, p, a, b); }
 };
 
 // Operations that run first after the MIXED replacement slot clear the
@@ -345,8 +377,12 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         const uint32_t bar = smem_u32(&bars[st]);
         mbar_arrive_expect_tx(bar, (uint32_t)SL::tx_bytes());
 #pragma unroll
-        for (int s = 0; s < SL::N; ++s)
-            tma_load_3d(stage0 + st * SB + SL::off(s), op.tmap[s], x0 - box_off(SL::esz(s)), y0 - 1, pa + q, bar);
+        for (int s = 0; s < SL::N; ++s) {
+            if (SL::interior(s))
+                tma_load_3d(stage0 + st * SB + SL::off(s), op.tmap[s], x0, y0, pa + q, bar);
+            else
+                tma_load_3d(stage0 + st * SB + SL::off(s), op.tmap[s], x0 - box_off(SL::esz(s)), y0 - 1, pa + q, bar);
+        }
     };
     if (tid == 0) {
         const int n0 = min(NSTAGE, NP);
@@ -409,7 +445,7 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         }
         if (out_plane && hkind == 1) {
             V a, b;
-            Op::load2(stage, p_halo, a, b);
+            HaloLoad<Op>::pair(stage, p_halo, a, b);
             const T f0 = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
             const T f1 = h1 ? op.field(g, C, S, b, Pos{hgx + 1, hgy, zq, hbc1 + bcz}) : T(0);
             *reinterpret_cast<Pair<T> *>(&fb[zq % 3][hrow][hcol]) = Pair<T>{f0, f1};
@@ -789,7 +825,7 @@ struct OpCG1 {
         f = v.p * beta + v.r * inv;  // as field()
         return Own{v.code, d};
     }
-    __device__ Out apply(const Geo &, const Coef<T> &, Shared &, const Own &o, const Pos &, T fc,
+    __device__ Out apply(const Geo &, const Coef<T> &C, Shared &, const Own &o, const Pos &, T fc,
                          T fxp, T fxm, T fyp, T fym, T fzp, T fzm)
     {
         const T q = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, o.d);
@@ -819,7 +855,8 @@ struct OpCG2 {
     using T = TT;
     static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
     static constexpr uint32_t wait_hint_ns = FB ? FAST_TAU_HINT_CG : 0;
-    using SL = Streams<sizeof(TT), sizeof(TT), sizeof(TT), 1>;
+    // p (halo), x and r (own points only), code
+    using SL = Streams<sizeof(TT), own_only(sizeof(TT)), own_only(sizeof(TT)), 1>;
     static constexpr int NV = 2;
     using Shared = NoShared;
     struct Vals { T p, x, r; uint32_t code; };
@@ -840,14 +877,18 @@ struct OpCG2 {
         sv2<T, SL, 2>(st, p, a.r, b.r);
         load_code2<SL, 3>(st, p, a.code, b.code);
     }
+    __device__ static void load2h(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<T, SL, 0>(st, p, a.p, b.p);
+    }
     __device__ static void load1(const unsigned char *st, const Pt &p, Vals &a) { a.p = sv<T, SL, 0>(st, p); }
     __device__ void init(const Job &J, Shared &)
     {
         F = faces_of<T>(J);
         const int par = (int)(J.sc->iter & 1);
         tmap[0] = &J.tm[TM_P + (par ^ 1)];
-        tmap[1] = &J.tm[TM_X];
-        tmap[2] = &J.tm[TM_R];
+        tmap[1] = &J.tm[FAST_TAU_INTERIOR ? TM_XI : TM_X];
+        tmap[2] = &J.tm[FAST_TAU_INTERIOR ? TM_RI : TM_R];
         tmap[3] = &J.tm[TM_CODE];
         x = (T *)J.x;
         r = (T *)J.r[0];
@@ -1304,7 +1345,7 @@ struct OpBiK1 {
     static constexpr bool FB = true;
     static constexpr bool clears_gate = true;
     static constexpr uint32_t wait_hint_ns = FAST_TAU_HINT_K1;
-    using SL = Streams<4, 4, 4, 4, 4, 4, 1>;  // r, v, t, p, e, r0, code
+    using SL = Streams<4, 4, 4, 4, own_only(4), own_only(4), 1>;  // r, v, t, p (halo), e, r0 (own points only), code
     static constexpr int NV = 2;
     using Shared = NoShared;
     struct Vals { float r, v, t, p, e, r0; uint32_t code; };
@@ -1336,6 +1377,14 @@ struct OpBiK1 {
         a.p = sv<float, SL, 3>(st, p);
         a.code = sv<uint8_t, SL, 6>(st, p);
     }
+    __device__ static void load2h(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<float, SL, 0>(st, p, a.r, b.r);
+        sv2<float, SL, 1>(st, p, a.v, b.v);
+        sv2<float, SL, 2>(st, p, a.t, b.t);
+        sv2<float, SL, 3>(st, p, a.p, b.p);
+        load_code2<SL, 6>(st, p, a.code, b.code);
+    }
     __device__ void init(const Job &J, Shared &)
     {
         F = faces_of<T>(J);
@@ -1345,8 +1394,8 @@ struct OpBiK1 {
         tmap[1] = &J.tm[TM_V + par];
         tmap[2] = &J.tm[TM_T];
         tmap[3] = &J.tm[TM_P + par];
-        tmap[4] = &J.tm[TM_X];
-        tmap[5] = &J.tm[TM_R0];
+        tmap[4] = &J.tm[FAST_TAU_INTERIOR ? TM_XI : TM_X];
+        tmap[5] = &J.tm[FAST_TAU_INTERIOR ? TM_R0I : TM_R0];
         tmap[6] = &J.tm[TM_CODE];
         rnew = (float *)J.r[par ^ 1];
         pnew = (float *)J.p[par ^ 1];
@@ -1381,7 +1430,7 @@ struct OpBiK1 {
                          T fyp, T fym, T fzp, T fzm)
     {
         const T d = diag_of<T, FB>(C, g, o.code, ps);
-        const T vn = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T vn = stencil7t<T>(F, C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         r0v.add_prod(o.r0, vn);
         rr.add_prod(o.rk, o.rk);
         return Out{o.rk, o.pk, vn, o.e};
@@ -1401,7 +1450,7 @@ struct OpBiK2 {
     using T = float;
     static constexpr bool FB = true;
     static constexpr uint32_t wait_hint_ns = FAST_TAU_HINT_K2;
-    using SL = Streams<4, 4, 4, 1>;  // r, v, r0, code
+    using SL = Streams<4, 4, own_only(4), 1>;  // r, v (halo), r0 (own points only), code
     static constexpr int NV = 4;
     using Shared = NoShared;
     struct Vals { float r, v, r0; uint32_t code; };
@@ -1428,13 +1477,19 @@ struct OpBiK2 {
         a.v = sv<float, SL, 1>(st, p);
         a.code = sv<uint8_t, SL, 3>(st, p);
     }
+    __device__ static void load2h(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
+    {
+        sv2<float, SL, 0>(st, p, a.r, b.r);
+        sv2<float, SL, 1>(st, p, a.v, b.v);
+        load_code2<SL, 3>(st, p, a.code, b.code);
+    }
     __device__ void init(const Job &J, Shared &)
     {
         F = faces_of<T>(J);
         const int par = (int)(J.sc->iter & 1);  // step 1 has counted the iteration
         tmap[0] = &J.tm[TM_R + par];
         tmap[1] = &J.tm[TM_V + par];
-        tmap[2] = &J.tm[TM_R0];
+        tmap[2] = &J.tm[FAST_TAU_INTERIOR ? TM_R0I : TM_R0];
         tmap[3] = &J.tm[TM_CODE];
         tout = (float *)J.t;
         nalpha = (float)(-J.sc->alpha);
@@ -1453,7 +1508,7 @@ struct OpBiK2 {
                          T fyp, T fym, T fzp, T fzm)
     {
         const T d = diag_of<T, FB>(C, g, o.code, ps);
-        const T t = stencil7<T>(F, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T t = stencil7t<T>(F, C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         ts.add_prod(t, o.s);
         tt.add_prod(t, t);
         r0t.add_prod(o.r0, t);

@@ -40,7 +40,10 @@ enum SolveState : int32_t {
 // Tensor maps of a job's arrays (TMA descriptors), by array.
 enum TensorMapId : int {
     TM_CODE = 0, TM_X = 1, TM_R = 2 /* +parity */, TM_R0 = 4, TM_P = 5 /* +parity */, TM_V = 7 /* +parity */,
-    TM_X64 = 9 /* +parity */, TM_T = 11, NTM = 12
+    TM_X64 = 9 /* +parity */, TM_T = 11,
+    // the same arrays with the TX x TY tile as the box (streams read only at
+    // a block's own points): x, r[0], r0
+    TM_XI = 12, TM_RI = 13, TM_R0I = 14, NTM = 15
 };
 
 // Per right-hand-side solver scalars, resident in device memory and updated
