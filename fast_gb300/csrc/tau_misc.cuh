@@ -27,8 +27,23 @@ struct XArith<double> {
     {
         return stencil7<double>(F, code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag_of<double, false>(C, g, code, ps));
     }
-    __device__ static float residual32(double b, double ax) { return (float)(b - ax); }
-    __device__ static float to_float(double v) { return (float)v; }
+    // fp32(b - A x) and fp32(b).  b is nonzero only on the first and last
+    // plane of the primary axis (where it is exact in FP32); elsewhere the
+    // residual is -A x, with no FP64 subtraction and no conversion of b (the
+    // FP64 pipe bounds this kernel).
+    __device__ static void residual(const Tab &C, const Geo &g, uint32_t code, const Pos &ps, double ax, float &r32,
+                                    float &b32)
+    {
+        const int c = g.coord(ps.x, ps.y, ps.z);
+        if (c == 0 || c == g.extent() - 1) {
+            const double b = rhs_at<double>(C, g, code, ps.x, ps.y, ps.z);
+            r32 = (float)(b - ax);
+            b32 = (float)b;
+        } else {
+            r32 = (float)(-ax);
+            b32 = 0.f;
+        }
+    }
 };
 
 template <>
@@ -40,8 +55,13 @@ struct XArith<FF> {
     {
         return stencil7_ff(F, code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag_ff(C, code, ps));
     }
-    __device__ static float residual32(FF b, FF ax) { return ff_to_float(ff_add(b, ff_neg(ax))); }
-    __device__ static float to_float(FF v) { return ff_to_float(v); }
+    __device__ static void residual(const Tab &C, const Geo &g, uint32_t code, const Pos &ps, FF ax, float &r32,
+                                    float &b32)
+    {
+        const FF b = rhs_at<FF>(C, g, code, ps.x, ps.y, ps.z);
+        r32 = ff_to_float(ff_add(b, ff_neg(ax)));
+        b32 = ff_to_float(b);
+    }
 };
 
 // ===========================================================================
@@ -122,9 +142,8 @@ struct OpReplace {
                          XT fxp, XT fxm, XT fyp, XT fym, XT fzp, XT fzm)
     {
         const XT ax = X::stencil(F, C, g, o.code, ps, fc, fxp, fxm, fyp, fym, fzp, fzm);
-        const XT b = rhs_at<XT>(C, g, o.code, ps.x, ps.y, ps.z);
-        const float r32 = X::residual32(b, ax);
-        const float b32 = X::to_float(b);
+        float r32, b32;
+        X::residual(C, g, o.code, ps, ax, r32, b32);
         a_rr.add_prod(r32, r32);
         a_bb.add_prod(b32, b32);
         if constexpr (BICG) {
@@ -291,9 +310,8 @@ struct OpReplaceBi2 {
                          XT fxp, XT fxm, XT fyp, XT fym, XT fzp, XT fzm)
     {
         const XT ax = X::stencil(F, C, g, o.code, ps, fc, fxp, fxm, fyp, fym, fzp, fzm);
-        const XT b = rhs_at<XT>(C, g, o.code, ps.x, ps.y, ps.z);
-        const float r32 = X::residual32(b, ax);
-        const float b32 = X::to_float(b);
+        float r32, b32;
+        X::residual(C, g, o.code, ps, ax, r32, b32);
         a_rr.add_prod(r32, r32);
         a_bb.add_prod(b32, b32);
         a_d.add_prod(restart ? r32 : o.r0, r32);
