@@ -628,12 +628,16 @@ def c4_requests(n, seed=2024, pool=0):
     return specs, masks
 
 
-def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0):
+def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0, max_pending=256):
     """Serving stream: Poisson arrivals of c4_requests(n_requests) at each
     rate into one TauServer (MIXED, tol 1e-6); latency = completion minus
     arrival; against the plain drop-in solver (FP64, one request per call,
     back to back) on the same requests (all, or `plain_sample` of them evenly
-    spaced through the stream so the sample keeps its size mix)."""
+    spaced through the stream so the sample keeps its size mix).  Requests
+    that have arrived wait on the client side (their buffers uncopied) while
+    `max_pending` submitted requests are still queued in the server, so an
+    overloaded stream does not hold a host copy of every waiting volume;
+    their latency still counts from their arrival."""
     import torch
     import fast_gb300 as ft
     from fast_gb300.serve import TauServer
@@ -651,9 +655,11 @@ def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0):
             done = []
             while k < len(masks) or srv.busy():
                 now = srv.now() - t0
-                while k < len(masks) and arrivals[k] <= now:
+                room = max_pending - srv.stats()["pending"] if max_pending > 0 else len(masks)
+                while k < len(masks) and arrivals[k] <= now and room > 0:
                     srv.submit(masks[k], ft.Dir(specs[k]["dir"]), ft.DiffusionSolverType(specs[k]["solver"]))
                     k += 1
+                    room -= 1
                 if srv.busy():
                     done.extend(srv.poll())
                 elif k < len(masks):
@@ -686,7 +692,8 @@ def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0):
             "generation_seconds": t_gen,
             "mix": "edge log-U[32,384] cubic, spheres r U[3,8] or ellipsoids aspect U[0.1,1], "
                    "solid U[0.40,0.75], dir U(6), CG or BiCGSTAB",
-            "server": "TauServer MIXED tol 1e-6, 16-iteration chunks, admission by HBM footprint"}
+            "server": "TauServer MIXED tol 1e-6, 16-iteration chunks, admission by HBM footprint",
+            "client_queue": f"arrived requests wait uncopied while {max_pending} are queued in the server"}
 
 
 def run_c4(args):
