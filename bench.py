@@ -671,6 +671,7 @@ def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0, max_pending=256
                                "p99_ms": 1e3 * float(np.percentile(lat, 99)),
                                "arrival_span_s": float(arrivals[-1] - arrivals[0]), "makespan_s": span,
                                "all_converged": all(c.result.status == ft.Status.OK for c in done)}
+        print(json.dumps({"c4_rate": rate, **out[str(int(rate))]}), file=sys.stderr, flush=True)
     n = len(masks)
     picks = list(range(n)) if plain_sample <= 0 or plain_sample >= n else \
         sorted({int(i) for i in np.linspace(0, n - 1, plain_sample)})
