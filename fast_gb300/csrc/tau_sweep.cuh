@@ -301,6 +301,11 @@ struct GateRole<Op, std::void_t<decltype(Op::clears_gate)>> {
 // or SWEEP_FAULT.
 enum { SWEEP_DONE = 0, SWEEP_IDLE = 1, SWEEP_FAULT = 2 };
 
+#ifndef FAST_TAU_REFILL_THREAD
+#define FAST_TAU_REFILL_THREAD (NTHREADS - 32)
+#endif
+constexpr int kRefillThread = FAST_TAU_REFILL_THREAD;
+
 template <class Op, int NSTAGE>
 __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb, bool &ready, int64_t *idle_end)
 {
@@ -457,7 +462,8 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         __syncthreads();
         if (s_err) break;
         // Every thread is done with this stage: refill it with plane q+NSTAGE.
-        if (tid == 0 && q + NSTAGE < NP) {
+        // The last warp issues (the first warps also load the halo rows).
+        if (tid == kRefillThread && q + NSTAGE < NP) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(q + NSTAGE);
         }
