@@ -628,7 +628,7 @@ def c4_requests(n, seed=2024, pool=0):
     return specs, masks
 
 
-def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0, max_pending=256):
+def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0, max_pending=256, progress=False):
     """Serving stream: Poisson arrivals of c4_requests(n_requests) at each
     rate into one TauServer (MIXED, tol 1e-6); latency = completion minus
     arrival; against the plain drop-in solver (FP64, one request per call,
@@ -671,7 +671,10 @@ def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0, max_pending=256
                                "p99_ms": 1e3 * float(np.percentile(lat, 99)),
                                "arrival_span_s": float(arrivals[-1] - arrivals[0]), "makespan_s": span,
                                "all_converged": all(c.result.status == ft.Status.OK for c in done)}
-        print(json.dumps({"c4_rate": rate, **out[str(int(rate))]}), file=sys.stderr, flush=True)
+        if progress:
+            r_ = out[str(int(rate))]
+            print(f"c4 rate {rate:g}/s: {r_['solves_per_s']:.2f} solves/s, p50 {r_['p50_ms'] / 1e3:.1f} s, "
+                  f"p99 {r_['p99_ms'] / 1e3:.1f} s", file=sys.stderr, flush=True)
     n = len(masks)
     picks = list(range(n)) if plain_sample <= 0 or plain_sample >= n else \
         sorted({int(i) for i in np.linspace(0, n - 1, plain_sample)})
@@ -699,7 +702,7 @@ def c4_record(n_requests, rates, plain_sample, chunk=16, pool=0, max_pending=256
 
 def run_c4(args):
     import fast_gb300  # noqa: F401
-    rec = c4_record(args.requests, args.rates, args.plain_sample, pool=args.c4_pool)
+    rec = c4_record(args.requests, args.rates, args.plain_sample, pool=args.c4_pool, progress=True)
     best = rec["best_solves_per_s"]
     line = _line("tau solves/s", best, "solves/s", args, 1e3 / best, "f32+f64",
                  {"workload": "c4_serving_stream", "requests": rec["requests"], "mix": rec["mix"], "tol": 1e-6,
