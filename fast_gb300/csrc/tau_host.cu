@@ -684,6 +684,17 @@ int solve_jobs(Engine &E, const std::vector<VolSpec> &vols, const std::vector<Jo
     const size_t need = solve_bytes(vols, jobs, prec, solver, zc);
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
+#if defined(FAST_TAU_TEST_HOOKS) && FAST_TAU_TEST_HOOKS
+    // test builds: FAST_TAU_TEST_FREE_BYTES pretends the device has that much
+    // free memory and nothing cached, so the fit check can be made to fail
+    const char *fake_free = getenv("FAST_TAU_TEST_FREE_BYTES");
+    if (fake_free) {
+        free_b = (size_t)strtoull(fake_free, nullptr, 10);
+        if (need > free_b)
+            return fail(FAST_NOMEM, "Solver will not fit in GPU memory: needs %.3f GB, %.3f GB free", need / 1e9,
+                        free_b / 1e9);
+    }
+#endif
     if (need > free_b) {
         // Memory already cached by the stream-ordered pool counts as available.
         size_t reserved = 0;

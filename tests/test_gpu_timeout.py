@@ -13,7 +13,10 @@ one block, so the wait for them runs out), and checks, in a child process:
     FAST_TIMEOUT, the other two return the same tau as an unarmed call;
   * MIXED BiCGSTAB (the first sweep is the replacement kernel that walks
     tiles with a resident grid): the armed call returns FAST_TIMEOUT;
-  * the next call in the same process succeeds with the unarmed results.
+  * the next call in the same process succeeds with the unarmed results;
+  * with the device's free memory faked small (FAST_TAU_TEST_FREE_BYTES), a
+    solve fails with FAST_NOMEM before any device work, as the reference's
+    fit check makes it fail.
 
 No wait is unbounded and nothing traps: the failure is a status.
 """
@@ -48,6 +51,10 @@ def solve(dirs, prec, solver, arm=None):
     return [int(st), [[int(r.status), r.tau] for r in res]]
 
 out = {}
+os.environ["FAST_TAU_TEST_FREE_BYTES"] = "1000000"
+out["nomem"] = solve([0], ft.Precision.F64, ft.DSOLVER_CG)
+out["nomem_msg"] = _native.last_error()
+os.environ.pop("FAST_TAU_TEST_FREE_BYTES")
 out["f64_armed"] = solve([0, 2, 4], ft.Precision.F64, ft.DSOLVER_CG, arm=2)
 out["f64_after"] = solve([0, 2, 4], ft.Precision.F64, ft.DSOLVER_CG)
 out["mixed_armed"] = solve([1], ft.Precision.MIXED, ft.DSOLVER_BICGSTAB, arm=1)
@@ -56,7 +63,7 @@ out["mixed_plain"] = solve([1], ft.Precision.MIXED, ft.DSOLVER_BICGSTAB)
 print(json.dumps(out))
 """
 
-FAST_OK, FAST_TIMEOUT = 0, 7
+FAST_OK, FAST_NOMEM, FAST_TIMEOUT = 0, 3, 7
 
 
 @pytest.fixture(scope="module")
@@ -82,6 +89,10 @@ def test_withheld_tile_load_times_out_and_context_recovers(gpu, hooked_lib):
                        timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     out = json.loads(r.stdout.strip().splitlines()[-1])
+
+    # the reference's fit check (VolumeMeasures.cpp:104-125): a solve that
+    # does not fit fails with FAST_NOMEM before touching the device
+    assert out["nomem"][0] == FAST_NOMEM and "will not fit" in out["nomem_msg"]
 
     st, res = out["f64_armed"]
     st_after, res_after = out["f64_after"]
