@@ -162,7 +162,7 @@ int retire(Ctx &C, Scalars *snap, uint64_t seq, fast_ctx_completion *out, int32_
         int64_t nb = 0;
         int s = upload_jobs(C, C.h_stage, jobs, C.d_tmp[0], nb);
         if (s != FAST_OK) return s;
-        const Launch L{C.d_tmp[0], (int32_t)jobs.size(), 0, nb};
+        const Launch L{C.d_tmp[0], (int32_t)jobs.size(), 0, nb, nullptr};
         const int prec = C.cfg.precision;
         launch_tau(prec == FAST_PREC_MIXED ? 3 : (prec == FAST_PREC_F32 ? 1 : 0), L, C.st);
         SV(cudaGetLastError());
@@ -270,9 +270,9 @@ int admit(Ctx &C)
     int64_t nb = 0;
     int s = upload_jobs(C, C.h_stage + C.kMax, jobs, C.d_tmp[1], nb);
     if (s != FAST_OK) return s;
-    launch_code(Launch{C.d_tmp[1], (int32_t)jobs.size(), 0, nb}, C.st);
+    launch_code(Launch{C.d_tmp[1], (int32_t)jobs.size(), 0, nb, nullptr}, C.st);
     if (C.cfg.precision == FAST_PREC_MIXED) {
-        launch_init64(Launch{C.d_tmp[1], (int32_t)jobs.size(), 0, nb}, C.st);
+        launch_init64(Launch{C.d_tmp[1], (int32_t)jobs.size(), 0, nb, nullptr}, C.st);
     } else {
         for (int g = 0; g < 2; g++) {
             std::vector<const Job *> gj;
@@ -282,7 +282,7 @@ int admit(Ctx &C)
             int64_t gb = 0;
             s = upload_jobs(C, C.h_stage + (2 + g) * C.kMax, gj, C.d_tmp[2 - g], gb);
             if (s != FAST_OK) return s;
-            dispatch(C, g == FAST_SOLVER_CG ? Step::INIT_CG : Step::INIT_BI, Launch{C.d_tmp[2 - g], (int32_t)gj.size(), 0, gb},
+            dispatch(C, g == FAST_SOLVER_CG ? Step::INIT_CG : Step::INIT_BI, Launch{C.d_tmp[2 - g], (int32_t)gj.size(), 0, gb, nullptr},
                      C.st);
         }
     }

@@ -1155,7 +1155,7 @@ FAST_API int fast_porosity(const uint8_t *mask, int64_t nx, int64_t ny, int64_t 
     CU(cudaMemcpyAsync(d_job, &J, sizeof(Job), cudaMemcpyHostToDevice, s));
     CU(cudaMemsetAsync(d_sc, 0, sizeof(Scalars), s));
     CU(cudaMemsetAsync(d_cnt, 0, sizeof(uint32_t), s));
-    Launch L{d_job, 1, 0, G.ntiles};
+    Launch L{d_job, 1, 0, G.ntiles, nullptr};
     launch_code(L, s);
     CU(cudaMemcpyAsync(E->h_sc, d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
     cudaFreeAsync(A.base, s);
