@@ -950,7 +950,8 @@ def main():
     ap.add_argument("--no-subrecords", action="store_true",
                     help="headline only: skip the large-volume (c5) and serving (c4) records of the default line")
     ap.add_argument("--c4-requests", type=int, default=200, help="requests of the serving record in the default line")
-    ap.add_argument("--c4-rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0, 2000.0])
+    ap.add_argument("--c4-rates", type=float, nargs="+", default=[10.0, 50.0, 200.0, 1000.0, 2000.0],
+                    help="serving record of the default line: arrival rates (1/s); 10/s is below saturation")
     ap.add_argument("--c4-plain-sample", type=int, default=24)
     ap.add_argument("--c4-pool", type=int, default=500,
                     help="c4: distinct volumes generated for the stream (request k uses volume k %% pool)")

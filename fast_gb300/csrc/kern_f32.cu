@@ -29,18 +29,48 @@ constexpr int kStagesCGF = FAST_TAU_STAGES_CGF;
 constexpr int kBlocksCGF = FAST_TAU_BLOCKS_CGF;
 constexpr int kBlocksK1 = 3;
 
-template <class Op, int NS = kStages>
+#ifndef FAST_TAU_STAGES_R2
+#define FAST_TAU_STAGES_R2 2
+#endif
+#ifndef FAST_TAU_MINB_R2
+#define FAST_TAU_MINB_R2 0
+#endif
+// A sweep with two rows per thread runs half-size blocks, which the fixed
+// shared memory of a block (plane buffers, tables) already limits to few
+// per SM: its stage ring is shorter, and FAST_TAU_MINB_R2 > 0 bounds its
+// registers to fit that many blocks per SM.
+template <class Op>
+constexpr int stages_of()
+{
+    return RowsPerThread<Op>::n == 2 ? FAST_TAU_STAGES_R2 : kStages;
+}
+template <class Op>
+constexpr int min_blocks_of()
+{
+    return RowsPerThread<Op>::n == 2 ? FAST_TAU_MINB_R2 : 0;
+}
+
+template <class Op, int NS = stages_of<Op>()>
 static void go(const Launch &L, cudaStream_t st)
 {
     constexpr int dyn = sweep_dyn_smem<Op, NS>();
-    sweep_kernel<Op, NS><<<(unsigned)L.nblocks, NTHREADS, dyn, st>>>(L);
+    constexpr int MB = min_blocks_of<Op>();
+    if constexpr (MB > 0)
+        sweep_kernel_mb<Op, NS, MB><<<(unsigned)L.nblocks, sweep_threads<Op>(), dyn, st>>>(L);
+    else
+        sweep_kernel<Op, NS><<<(unsigned)L.nblocks, sweep_threads<Op>(), dyn, st>>>(L);
 }
 
-template <class Op, int NS = kStages>
+template <class Op, int NS = stages_of<Op>()>
 static cudaError_t cfg()
 {
-    return cudaFuncSetAttribute(sweep_kernel<Op, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                sweep_dyn_smem<Op, NS>());
+    constexpr int MB = min_blocks_of<Op>();
+    if constexpr (MB > 0)
+        return cudaFuncSetAttribute(sweep_kernel_mb<Op, NS, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    sweep_dyn_smem<Op, NS>());
+    else
+        return cudaFuncSetAttribute(sweep_kernel<Op, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    sweep_dyn_smem<Op, NS>());
 }
 
 template <typename ST>
@@ -97,11 +127,11 @@ void launch_mixed_inner(Step s, const Launch &L, cudaStream_t st)
 {
     if (s == Step::BI_K1)
         sweep_kernel_mb<OpBiK1, kStagesK1, kBlocksK1>
-            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpBiK1, kStagesK1>(), st>>>(L);
+            <<<(unsigned)L.nblocks, sweep_threads<OpBiK1>(), sweep_dyn_smem<OpBiK1, kStagesK1>(), st>>>(L);
     else if (s == Step::BI_K2) go<OpBiK2>(L, st);
     else if (s == Step::CG_F)
         sweep_kernel_mb<OpCGF, kStagesCGF, kBlocksCGF>
-            <<<(unsigned)L.nblocks, NTHREADS, sweep_dyn_smem<OpCGF, kStagesCGF>(), st>>>(L);
+            <<<(unsigned)L.nblocks, sweep_threads<OpCGF>(), sweep_dyn_smem<OpCGF, kStagesCGF>(), st>>>(L);
     else dispatch<double>(s, L, st);
 }
 

@@ -14,7 +14,7 @@ template <class Op>
 static void go(const Launch &L, cudaStream_t st)
 {
     constexpr int dyn = sweep_dyn_smem<Op, kStages>();
-    sweep_kernel<Op, kStages><<<(unsigned)L.nblocks, NTHREADS, dyn, st>>>(L);
+    sweep_kernel<Op, kStages><<<(unsigned)L.nblocks, sweep_threads<Op>(), dyn, st>>>(L);
 }
 
 template <class Op>

@@ -16,7 +16,7 @@ template <class Op>
 static void launch_tiles(const Launch &L, cudaStream_t st, int64_t resident)
 {
     const unsigned grid = (unsigned)(L.nblocks < resident ? L.nblocks : resident);
-    sweep_kernel_tiles<Op, kStages><<<grid, NTHREADS, sweep_dyn_smem<Op, kStages>(), st>>>(L);
+    sweep_kernel_tiles<Op, kStages><<<grid, sweep_threads<Op>(), sweep_dyn_smem<Op, kStages>(), st>>>(L);
 }
 
 void launch_replace(bool bicg, bool ff, const Launch &L, cudaStream_t st)
@@ -38,7 +38,7 @@ static cudaError_t configure_tiles(int &resident)
                                          sweep_dyn_smem<Op, kStages>());
     int per_sm = 0, dev = 0, sms = 0;
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel_tiles<Op, kStages>, NTHREADS,
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel_tiles<Op, kStages>, sweep_threads<Op>(),
                                                           sweep_dyn_smem<Op, kStages>());
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

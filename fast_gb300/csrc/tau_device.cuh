@@ -90,16 +90,30 @@ struct Coef<float> {
     float face[2][2];
     float cell2[2];
     float2 di[NBC][128];  // {diag, 1/diag} by (boundary count + 2, code)
-#if FAST_TAU_FACE_TABLE
-    // The six face coefficients of a stencil code (X+, X-, Y+, Y-, Z+, Z-):
-    // face[self solid][neighbour solid] selected by the code's bits.
-    float4 fxy[128];
-    float2 fz[128];
-#endif
 };
 
+// The six face coefficients of each stencil code (X+, X-, Y+, Y-, Z+, Z-):
+// face[self solid][neighbour solid] selected by the code's bits.  Shared
+// memory of the sweeps that read it (FAST_TAU_FACE_TABLE), not of the others.
+struct FaceTable {
+    float4 fxy[128];
+    float2 fz[128];
+};
+
+// Fills the table (blocks of at least 128 threads).
+__device__ __forceinline__ void load_face_table(FaceTable &t, const Job &J, int tid)
+{
+    if (tid < 128) {
+        const int self = (tid >> SELF_BIT) & 1;
+        auto f = [&](int d) { return J.fface[self][(tid >> d) & 1]; };
+        t.fxy[tid] = make_float4(f(0), f(1), f(2), f(3));
+        t.fz[tid] = make_float2(f(4), f(5));
+    }
+}
+
+// Fills the block's coefficient tables; nt = the block's threads.
 template <typename T>
-__device__ __forceinline__ void load_coef(Coef<T> &C, const Job &J, int tid)
+__device__ __forceinline__ void load_coef(Coef<T> &C, const Job &J, int tid, int nt = NTHREADS)
 {
     if constexpr (sizeof(T) == 8) {
         if (tid < 128) {
@@ -109,18 +123,10 @@ __device__ __forceinline__ void load_coef(Coef<T> &C, const Job &J, int tid)
         if (tid < 4) C.face[tid >> 1][tid & 1] = J.dface[tid >> 1][tid & 1];
         if (tid < 2) C.cell2[tid] = 2.0 * J.dcell[tid];
     } else {
-        for (int k = tid; k < NBC * 128; k += NTHREADS)
+        for (int k = tid; k < NBC * 128; k += nt)
             C.di[k >> 7][k & 127] = make_float2(J.fdiag_b[k >> 7][k & 127], J.finv_b[k >> 7][k & 127]);
         if (tid < 4) C.face[tid >> 1][tid & 1] = J.fface[tid >> 1][tid & 1];
         if (tid < 2) C.cell2[tid] = (float)(2.0 * J.dcell[tid]);
-#if FAST_TAU_FACE_TABLE
-        if (tid < 128) {
-            const int self = (tid >> SELF_BIT) & 1;
-            auto f = [&](int d) { return J.fface[self][(tid >> d) & 1]; };
-            C.fxy[tid] = make_float4(f(0), f(1), f(2), f(3));
-            C.fz[tid] = make_float2(f(4), f(5));
-        }
-#endif
     }
 }
 
@@ -134,9 +140,9 @@ struct Coef<FF> {
 };
 
 template <>
-__device__ __forceinline__ void load_coef<FF>(Coef<FF> &C, const Job &J, int tid)
+__device__ __forceinline__ void load_coef<FF>(Coef<FF> &C, const Job &J, int tid, int nt)
 {
-    for (int k = tid; k < NBC * 128; k += NTHREADS) {
+    for (int k = tid; k < NBC * 128; k += nt) {
         C.dhi[k >> 7][k & 127] = J.xdiag_hi[k >> 7][k & 127];
         C.dlo[k >> 7][k & 127] = J.xdiag_lo[k >> 7][k & 127];
     }
@@ -364,18 +370,18 @@ __device__ __forceinline__ T stencil7(const Faces<T> &F, uint32_t code, T fc, T 
 }
 
 // The stencil with the six face coefficients of the code taken from one
-// shared-memory table entry (FP32, FAST_TAU_FACE_TABLE) instead of selected
-// by its code bits: the same products in the same order, so the same result.
-// Measured per kernel: faster for the BiCGSTAB sweeps, slower for the PCG
-// sweeps, which keep the bit selects (stencil7).
+// shared-memory table entry (FP32) instead of selected by its code bits: the
+// same products in the same order, so the same result.  Measured per kernel:
+// faster for the BiCGSTAB sweeps, slower for the PCG sweeps, which keep the
+// bit selects (stencil7).
 template <typename T>
-__device__ __forceinline__ T stencil7t(const Faces<T> &F, const Coef<T> &C, uint32_t code, T fc, T fxp, T fxm, T fyp,
-                                       T fym, T fzp, T fzm, T diag)
+__device__ __forceinline__ T stencil7t(const FaceTable &t, uint32_t code, T fc, T fxp, T fxm, T fyp, T fym, T fzp,
+                                       T fzm, T diag)
 {
-#if FAST_TAU_FACE_TABLE
-    if constexpr (std::is_same<T, float>::value) {
-        const float4 q = C.fxy[code & 127];
-        const float2 r = C.fz[code & 127];
+    static_assert(std::is_same<T, float>::value, "FP32 table");
+    {
+        const float4 q = t.fxy[code & 127];
+        const float2 r = t.fz[code & 127];
         T s = fxp * q.x;
         s += fxm * q.y;
         s += fyp * q.z;
@@ -385,9 +391,6 @@ __device__ __forceinline__ T stencil7t(const Faces<T> &F, const Coef<T> &C, uint
         s += fc * diag;
         return s;
     }
-#endif
-    (void)C;
-    return stencil7<T>(F, code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag);
 }
 
 // The same stencil in float-float arithmetic (the MIXED residual
@@ -511,13 +514,13 @@ __device__ __forceinline__ FF diag_ff(const Coef<FF> &C, uint32_t code, const Po
 
 // Sum NV per-thread values over the block (fixed tree) and store the block
 // totals, as doubles, to out[0..NV).  FP32 values are combined as
-// compensated (sum, error) pairs.
-template <int NV, typename V>
-__device__ __forceinline__ void block_sum_store(const V (&v)[NV], double *out, double *s_red /* [NV][2*NTHREADS/32] */)
+// compensated (sum, error) pairs.  NT = the block's threads.
+template <int NV, typename V, int NT = NTHREADS>
+__device__ __forceinline__ void block_sum_store(const V (&v)[NV], double *out, double *s_red /* [NV][2*NT/32] */)
 {
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
-    constexpr int NW = NTHREADS / 32;
+    constexpr int NW = NT / 32;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
         if constexpr (sizeof(V) == 8) {
@@ -570,7 +573,7 @@ __device__ __forceinline__ bool arrive_last(uint32_t *counter, int64_t ntiles, i
     return *s_flag != 0;
 }
 
-template <int NV>
+template <int NV, int NT = NTHREADS>
 __device__ __forceinline__ void sum_partials(const double *part, int64_t ntiles, double (&tot)[NV], double *s_red)
 {
     const int tid = threadIdx.x;
@@ -578,12 +581,12 @@ __device__ __forceinline__ void sum_partials(const double *part, int64_t ntiles,
     double v[NV];
 #pragma unroll
     for (int k = 0; k < NV; k++) v[k] = 0.0;
-    for (int64_t t = tid; t < ntiles; t += NTHREADS) {
+    for (int64_t t = tid; t < ntiles; t += NT) {
 #pragma unroll
         for (int k = 0; k < NV; k++) v[k] += __ldcg(part + t * NPART + k);
     }
     __shared__ double s_tot[NV];
-    block_sum_store<NV, double>(v, s_tot, s_red);
+    block_sum_store<NV, double, NT>(v, s_tot, s_red);
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < NV; k++) tot[k] = s_tot[k];

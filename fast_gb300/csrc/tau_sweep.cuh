@@ -301,10 +301,28 @@ struct GateRole<Op, std::void_t<decltype(Op::clears_gate)>> {
 // or SWEEP_FAULT.
 enum { SWEEP_DONE = 0, SWEEP_IDLE = 1, SWEEP_FAULT = 2 };
 
-#ifndef FAST_TAU_REFILL_THREAD
-#define FAST_TAU_REFILL_THREAD (NTHREADS - 32)
-#endif
-constexpr int kRefillThread = FAST_TAU_REFILL_THREAD;
+// Rows per thread: an operation that names RPT = 2 sweeps its TX x TY tile
+// with half the threads, each owning two neighbouring rows of its two
+// columns (four points per plane).  The per-plane work that does not depend
+// on the point (ring slot and phase, the wait, plane indices, the barrier,
+// store addresses) is then spread over twice the points, and the y
+// neighbour inside a thread's row pair comes from its registers.  For the
+// sweeps whose few bytes per point leave them bound by instruction issue.
+template <class Op, class = void>
+struct RowsPerThread {
+    static constexpr int n = 1;
+};
+template <class Op>
+struct RowsPerThread<Op, std::void_t<decltype(Op::RPT)>> {
+    static constexpr int n = Op::RPT;
+};
+
+// Threads of an operation's sweep blocks.
+template <class Op>
+__host__ __device__ constexpr int sweep_threads()
+{
+    return NTHREADS / RowsPerThread<Op>::n;
+}
 
 template <class Op, int NSTAGE>
 __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb, bool &ready, int64_t *idle_end)
@@ -314,12 +332,19 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
     using V = typename Op::Vals;
     constexpr int NV = Op::NV;
     constexpr int SB = SL::stage_bytes();
+    constexpr int RPT = RowsPerThread<Op>::n;
+    constexpr int NT = sweep_threads<Op>();
+    static_assert((RPT == 1 || RPT == 2) && TY % RPT == 0, "one or two rows per thread");
+    static_assert(NT >= 2 * TPR + 2 * TY && NT % 32 == 0, "halo roles need 2 TPR + 2 TY threads");
+    // The stage refill: the first thread of the last warp (the first warps
+    // also form the halo rows).
+    constexpr int kRefillThread = NT - 32;
     extern __shared__ __align__(128) unsigned char dsm[];
     __shared__ __align__(8) uint64_t bars[NSTAGE];
     __shared__ int s_job, s_go, s_flag, s_err;
     __shared__ Coef<T> C;
     __shared__ __align__(16) T fb[3][HY][PW];
-    __shared__ double s_red[2 * NV * (NTHREADS / 32)];
+    __shared__ double s_red[2 * NV * (NT / 32)];
     __shared__ typename Op::Shared S;
 
     const int tid = threadIdx.x;
@@ -338,7 +363,7 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         return SWEEP_IDLE;
     }
     const Job &J = L.jobs[s_job];
-    load_coef<T>(C, J, tid);
+    load_coef<T>(C, J, tid, NT);
     Op::load_shared(S, J, tid);
 
     const Geo g{J.nx, J.ny, J.nz, J.dir >> 1, (J.dir & 1) ? -1 : 1, J.pitch};
@@ -351,12 +376,18 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
     const int z1 = min(z0 + J.zc, g.nz);
     const int pa = max(z0 - 1, 0), pb = min(z1, g.nz - 1);
     const int NP = pb - pa + 1;
-    const int lp = tid % TPR, ly = tid / TPR;
-    const int gx = x0 + 2 * lp, gy = y0 + ly;
-    const bool v0 = gx < g.nx && gy < g.ny;
-    const bool v1 = gx + 1 < g.nx && gy < g.ny;
+    // A thread's points: columns gx, gx + 1 of tile rows ly0 .. ly0 + RPT - 1.
+    const int lp = tid % TPR, ly0 = (tid / TPR) * RPT;
+    const int gx = x0 + 2 * lp;
+    bool v0[RPT], v1[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        v0[r] = gx < g.nx && y0 + ly0 + r < g.ny;
+        v1[r] = gx + 1 < g.nx && y0 + ly0 + r < g.ny;
+    }
+    const bool any_v = v0[0] || v1[0] || (RPT == 2 && (v0[RPT - 1] || v1[RPT - 1]));
     const int64_t plane = (int64_t)g.P * g.ny;
-    const int64_t i_col = (int64_t)gx + (int64_t)g.P * gy;
+    const int64_t i_col = (int64_t)gx + (int64_t)g.P * (y0 + ly0);
 
     Op op;
     op.init(J, S);
@@ -416,15 +447,69 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
     const bool hin_y = (unsigned)hgy < (unsigned)g.ny;
     const bool h0 = hin_y && (unsigned)hgx < (unsigned)g.nx;
     const bool h1 = hin_y && (unsigned)(hgx + 1) < (unsigned)g.nx;
-    const Pt p_own{ly + 1, 2 * lp};
     const Pt p_halo{hrow, hgx - x0};
     // Boundary counts in x and y of the thread's own columns and halo points
     // (fixed for the slab); the z part is added per plane.
-    const int bc0 = boundary_count_xy(g, gx, gy), bc1 = boundary_count_xy(g, gx + 1, gy);
+    int bc0[RPT], bc1[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        bc0[r] = boundary_count_xy(g, gx, y0 + ly0 + r);
+        bc1[r] = boundary_count_xy(g, gx + 1, y0 + ly0 + r);
+    }
     const int hbc0 = boundary_count_xy(g, hgx, hgy), hbc1 = boundary_count_xy(g, hgx + 1, hgy);
 
-    T fm0 = T(0), fm1 = T(0), fc0 = T(0), fc1 = T(0), fp0 = T(0), fp1 = T(0);
-    typename Op::Own oc0{}, oc1{}, op0{}, op1{};
+    // The field of the thread's points in the planes below (m), at (c) and
+    // above (p) the plane the operator is applied to, and the own-point
+    // state of the planes c and p.
+    T fm0[RPT], fm1[RPT], fc0[RPT], fc1[RPT], fp0[RPT], fp1[RPT];
+    typename Op::Own oc0[RPT], oc1[RPT], op0[RPT], op1[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        fm0[r] = fm1[r] = fc0[r] = fc1[r] = fp0[r] = fp1[r] = T(0);
+        oc0[r] = oc1[r] = op0[r] = op1[r] = typename Op::Own{};
+    }
+    // The operator at plane zs on the thread's points, from the plane
+    // buffer (x and y neighbours; the y neighbour inside the thread's row
+    // pair from its registers) and the field of the planes below (fm) and
+    // above (u0, u1: 0 past the last plane); stores the outputs.
+    auto apply_at = [&](int zs, const T(&u0)[RPT], const T(&u1)[RPT]) {
+        const int bczs = boundary_count_z(g, zs);
+        const T(*P)[PW] = fb[zs % 3];
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) {
+            if (!(v0[r] || v1[r])) continue;
+            const int row = ly0 + r + 1;
+            const Pair<T> left = *reinterpret_cast<const Pair<T> *>(&P[row][2 * lp]);
+            const Pair<T> right = *reinterpret_cast<const Pair<T> *>(&P[row][2 * lp + 4]);
+            T up0, up1, dn0, dn1;
+            if (r + 1 < RPT) {
+                up0 = fc0[r + 1];
+                up1 = fc1[r + 1];
+            } else {
+                const Pair<T> up = *reinterpret_cast<const Pair<T> *>(&P[row + 1][2 * lp + 2]);
+                up0 = up.a;
+                up1 = up.b;
+            }
+            if (r > 0) {
+                dn0 = fc0[r - 1];
+                dn1 = fc1[r - 1];
+            } else {
+                const Pair<T> dn = *reinterpret_cast<const Pair<T> *>(&P[row - 1][2 * lp + 2]);
+                dn0 = dn.a;
+                dn1 = dn.b;
+            }
+            const int gy = y0 + ly0 + r;
+            const int64_t i = i_col + (int64_t)r * g.P + plane * zs;
+            typename Op::Out o0{}, o1{};
+            if (v0[r])
+                o0 = op.apply(g, C, S, oc0[r], Pos{gx, gy, zs, bc0[r] + bczs}, fc0[r], fc1[r], left.b, up0, dn0, u0[r],
+                              fm0[r]);
+            if (v1[r])
+                o1 = op.apply(g, C, S, oc1[r], Pos{gx + 1, gy, zs, bc1[r] + bczs}, fc1[r], right.a, fc0[r], up1, dn1,
+                              u1[r], fm1[r]);
+            if (ft_in(J, i, i + 1, plane * g.nz, OOB_SWEEP_STORE)) op.store(i, o0, o1, v0[r], v1[r]);
+        }
+    };
     int q = 0;
     for (; q < NP; ++q) {
         const int zq = pa + q;
@@ -434,18 +519,20 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         const unsigned char *stage = sbase + st * SB;
         const bool out_plane = zq >= z0 && zq < z1;
         const int bcz = boundary_count_z(g, zq);
-        {
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) {
+            const int gy = y0 + ly0 + r;
             V a, b;
-            Op::load2(stage, p_own, a, b);
-            fp0 = T(0);
-            fp1 = T(0);
+            Op::load2(stage, Pt{ly0 + r + 1, 2 * lp}, a, b);
+            fp0[r] = T(0);
+            fp1[r] = T(0);
             if (out_plane) {
-                if (v0) op0 = op.own(g, C, S, a, Pos{gx, gy, zq, bc0 + bcz}, fp0);
-                if (v1) op1 = op.own(g, C, S, b, Pos{gx + 1, gy, zq, bc1 + bcz}, fp1);
-                *reinterpret_cast<Pair<T> *>(&fb[zq % 3][ly + 1][2 * lp + 2]) = Pair<T>{fp0, fp1};
+                if (v0[r]) op0[r] = op.own(g, C, S, a, Pos{gx, gy, zq, bc0[r] + bcz}, fp0[r]);
+                if (v1[r]) op1[r] = op.own(g, C, S, b, Pos{gx + 1, gy, zq, bc1[r] + bcz}, fp1[r]);
+                *reinterpret_cast<Pair<T> *>(&fb[zq % 3][ly0 + r + 1][2 * lp + 2]) = Pair<T>{fp0[r], fp1[r]};
             } else {
-                if (v0) fp0 = op.field(g, C, S, a, Pos{gx, gy, zq, bc0 + bcz});
-                if (v1) fp1 = op.field(g, C, S, b, Pos{gx + 1, gy, zq, bc1 + bcz});
+                if (v0[r]) fp0[r] = op.field(g, C, S, a, Pos{gx, gy, zq, bc0[r] + bcz});
+                if (v1[r]) fp1[r] = op.field(g, C, S, b, Pos{gx + 1, gy, zq, bc1[r] + bcz});
             }
         }
         if (out_plane && hkind == 1) {
@@ -468,25 +555,16 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
             issue(q + NSTAGE);
         }
         const int zs = zq - 1;
-        if (zs >= z0 && zs < z1 && (v0 || v1)) {
-            const int bczs = boundary_count_z(g, zs);
-            const T(*P)[PW] = fb[zs % 3];
-            const Pair<T> left = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp]);
-            const Pair<T> right = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp + 4]);
-            const Pair<T> up = *reinterpret_cast<const Pair<T> *>(&P[ly + 2][2 * lp + 2]);
-            const Pair<T> dn = *reinterpret_cast<const Pair<T> *>(&P[ly][2 * lp + 2]);
-            const int64_t i = i_col + plane * zs;
-            typename Op::Out r0{}, r1{};
-            if (v0) r0 = op.apply(g, C, S, oc0, Pos{gx, gy, zs, bc0 + bczs}, fc0, fc1, left.b, up.a, dn.a, fp0, fm0);
-            if (v1) r1 = op.apply(g, C, S, oc1, Pos{gx + 1, gy, zs, bc1 + bczs}, fc1, right.a, fc0, up.b, dn.b, fp1, fm1);
-            if (ft_in(J, i, i + 1, plane * g.nz, OOB_SWEEP_STORE)) op.store(i, r0, r1, v0, v1);
+        if (zs >= z0 && zs < z1 && any_v) apply_at(zs, fp0, fp1);
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) {
+            fm0[r] = fc0[r];
+            fm1[r] = fc1[r];
+            fc0[r] = fp0[r];
+            fc1[r] = fp1[r];
+            oc0[r] = op0[r];
+            oc1[r] = op1[r];
         }
-        fm0 = fc0;
-        fm1 = fc1;
-        fc0 = fp0;
-        fc1 = fp1;
-        oc0 = op0;
-        oc1 = op1;
     }
 
     if (s_err) {
@@ -502,29 +580,21 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
     }
     qb += NP;
     // The last plane of the volume has no z+1 neighbour: apply it here.
-    if (pb == z1 - 1 && (v0 || v1)) {
-        const int zs = z1 - 1;
-        const int bczs = boundary_count_z(g, zs);
-        const T(*P)[PW] = fb[zs % 3];
-        const Pair<T> left = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp]);
-        const Pair<T> right = *reinterpret_cast<const Pair<T> *>(&P[ly + 1][2 * lp + 4]);
-        const Pair<T> up = *reinterpret_cast<const Pair<T> *>(&P[ly + 2][2 * lp + 2]);
-        const Pair<T> dn = *reinterpret_cast<const Pair<T> *>(&P[ly][2 * lp + 2]);
-        typename Op::Out r0{}, r1{};
-        if (v0) r0 = op.apply(g, C, S, oc0, Pos{gx, gy, zs, bc0 + bczs}, fc0, fc1, left.b, up.a, dn.a, T(0), fm0);
-        if (v1) r1 = op.apply(g, C, S, oc1, Pos{gx + 1, gy, zs, bc1 + bczs}, fc1, right.a, fc0, up.b, dn.b, T(0), fm1);
-        const int64_t il = i_col + plane * zs;
-        if (ft_in(J, il, il + 1, plane * g.nz, OOB_SWEEP_STORE)) op.store(il, r0, r1, v0, v1);
+    if (pb == z1 - 1 && any_v) {
+        T zero[RPT];
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) zero[r] = T(0);
+        apply_at(z1 - 1, zero, zero);
     }
 
     using RT = typename RedType<Op>::type;
     RT v[NV];
     op.partials(v);
     if (!ft_in(J, local * NPART, local * NPART + NPART - 1, J.ntiles * NPART, OOB_PARTIALS)) return SWEEP_FAULT;
-    block_sum_store<NV, RT>(v, J.part + local * NPART, s_red);
+    block_sum_store<NV, RT, NT>(v, J.part + local * NPART, s_red);
     if (arrive_last(J.counter, J.ntiles, &s_flag)) {
         double tot[NV];
-        sum_partials<NV>(J.part, J.ntiles, tot, s_red);
+        sum_partials<NV, NT>(J.part, J.ntiles, tot, s_red);
         if (tid == 0) {
             for (int k = 0; k < NV && k < 4; k++) J.sc->dbg[k] = tot[k];
             Op::finish(*J.sc, tot);
@@ -539,7 +609,7 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
 // choice, or (for an operation that is otherwise held to two blocks per SM)
 // a bound that fits MB blocks.
 template <class Op, int NSTAGE>
-__global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
+__global__ void __launch_bounds__(sweep_threads<Op>()) sweep_kernel(Launch L)
 {
     int qb = 0;
     bool ready = false;
@@ -548,7 +618,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel(Launch L)
 }
 
 template <class Op, int NSTAGE, int MB>
-__global__ void __launch_bounds__(NTHREADS, MB) sweep_kernel_mb(Launch L)
+__global__ void __launch_bounds__(sweep_threads<Op>(), MB) sweep_kernel_mb(Launch L)
 {
     int qb = 0;
     bool ready = false;
@@ -561,7 +631,7 @@ __global__ void __launch_bounds__(NTHREADS, MB) sweep_kernel_mb(Launch L)
 // for operations that most launches leave idle (the residual replacement
 // slot of every iteration), so an idle launch costs one wave of blocks.
 template <class Op, int NSTAGE>
-__global__ void __launch_bounds__(NTHREADS) sweep_kernel_tiles(Launch L)
+__global__ void __launch_bounds__(sweep_threads<Op>()) sweep_kernel_tiles(Launch L)
 {
     // No replacement pending in the whole launch: leave without touching
     // the job table.
@@ -599,6 +669,29 @@ __global__ void __launch_bounds__(NTHREADS) sweep_kernel_tiles(Launch L)
 // ---------------------------------------------------------------------------
 struct NoShared {};
 struct NoOut {};
+
+// Shared memory of the sweeps that take the face coefficients of a point
+// from the per-code table (FAST_TAU_FACE_TABLE=1; else they select them by
+// the code's bits and hold nothing), and their stencil.
+#if FAST_TAU_FACE_TABLE
+using FaceShared = FaceTable;
+__device__ __forceinline__ void load_faces(FaceTable &t, const Job &J, int tid) { load_face_table(t, J, tid); }
+#else
+using FaceShared = NoShared;
+__device__ __forceinline__ void load_faces(NoShared &, const Job &, int) {}
+#endif
+
+__device__ __forceinline__ float stencil7s(const Faces<float> &F, const FaceShared &S, uint32_t code, float fc,
+                                           float fxp, float fxm, float fyp, float fym, float fzp, float fzm, float diag)
+{
+#if FAST_TAU_FACE_TABLE
+    (void)F;
+    return stencil7t<float>(S, code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag);
+#else
+    (void)S;
+    return stencil7<float>(F, code, fc, fxp, fxm, fyp, fym, fzp, fzm, diag);
+#endif
+}
 
 template <class SL, int S>
 __device__ __forceinline__ void load_code2(const unsigned char *st, const Pt &p, uint32_t &a, uint32_t &b)
@@ -775,10 +868,23 @@ __device__ __forceinline__ void mixed_bicg_finish(Scalars &sc, double r0r, doubl
 // CG.cu:113-135 (z, beta, p update of the previous iteration) + :70-81.
 // Streams: r, p_old, code.
 // ===========================================================================
+// Rows per thread of the MIXED FP32 sweeps (the PCG steps and BiCGSTAB
+// step 2); the other sweeps own one row per thread.
+#ifndef FAST_TAU_RPT_CG1
+#define FAST_TAU_RPT_CG1 2
+#endif
+#ifndef FAST_TAU_RPT_CG2
+#define FAST_TAU_RPT_CG2 2
+#endif
+#ifndef FAST_TAU_RPT_K2
+#define FAST_TAU_RPT_K2 1
+#endif
+
 template <typename TT, typename ST>
 struct OpCG1 {
     using T = TT;
     static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
+    static constexpr int RPT = FB ? FAST_TAU_RPT_CG1 : 1;
     static constexpr bool clears_gate = FB;
     static constexpr uint32_t wait_hint_ns = FB ? FAST_TAU_HINT_CG : 0;
     using SL = Streams<sizeof(TT), sizeof(TT), 1>;
@@ -860,6 +966,7 @@ template <typename TT, typename ST>
 struct OpCG2 {
     using T = TT;
     static constexpr bool FB = sizeof(TT) == 4 && sizeof(ST) == 8;  // MIXED FP32 iterations
+    static constexpr int RPT = FB ? FAST_TAU_RPT_CG2 : 1;
     static constexpr uint32_t wait_hint_ns = FB ? FAST_TAU_HINT_CG : 0;
     // p (halo), x and r (own points only), code
     using SL = Streams<sizeof(TT), own_only(sizeof(TT)), own_only(sizeof(TT)), 1>;
@@ -1353,7 +1460,7 @@ struct OpBiK1 {
     static constexpr uint32_t wait_hint_ns = FAST_TAU_HINT_K1;
     using SL = Streams<4, 4, 4, 4, own_only(4), own_only(4), 1>;  // r, v, t, p (halo), e, r0 (own points only), code
     static constexpr int NV = 2;
-    using Shared = NoShared;
+    using Shared = FaceShared;
     struct Vals { float r, v, t, p, e, r0; uint32_t code; };
     struct Own { uint32_t code; float rk, pk, e, r0; };
     struct Out { float r, p, v, e; };
@@ -1364,7 +1471,7 @@ struct OpBiK1 {
     Acc<float> r0v, rr;
 
     __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
-    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load_shared(Shared &S, const Job &J, int tid) { load_faces(S, J, tid); }
     __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
     {
         sv2<float, SL, 0>(st, p, a.r, b.r);
@@ -1432,11 +1539,11 @@ struct OpBiK1 {
         const float en = ce * (v.e + alpha * (v.p * inv) + omega * ((v.r - alpha * v.v) * inv));
         return Own{v.code, r, p, en, v.r0};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc, T fxp, T fxm,
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &S, const Own &o, const Pos &ps, T fc, T fxp, T fxm,
                          T fyp, T fym, T fzp, T fzm)
     {
         const T d = diag_of<T, FB>(C, g, o.code, ps);
-        const T vn = stencil7t<T>(F, C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T vn = stencil7s(F, S, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         r0v.add_prod(o.r0, vn);
         rr.add_prod(o.rk, o.rk);
         return Out{o.rk, o.pk, vn, o.e};
@@ -1455,10 +1562,11 @@ struct OpBiK1 {
 struct OpBiK2 {
     using T = float;
     static constexpr bool FB = true;
+    static constexpr int RPT = FAST_TAU_RPT_K2;
     static constexpr uint32_t wait_hint_ns = FAST_TAU_HINT_K2;
     using SL = Streams<4, 4, own_only(4), 1>;  // r, v (halo), r0 (own points only), code
     static constexpr int NV = 4;
-    using Shared = NoShared;
+    using Shared = FaceShared;
     struct Vals { float r, v, r0; uint32_t code; };
     struct Own { uint32_t code; float s, r0; };
     struct Out { float t; };
@@ -1469,7 +1577,7 @@ struct OpBiK2 {
     Acc<float> ts, tt, r0t, r0s;
 
     __device__ static bool active(const Scalars &sc) { return sc.state == RUNNING; }
-    __device__ static void load_shared(Shared &, const Job &, int) {}
+    __device__ static void load_shared(Shared &S, const Job &J, int tid) { load_faces(S, J, tid); }
     __device__ static void load2(const unsigned char *st, const Pt &p, Vals &a, Vals &b)
     {
         sv2<float, SL, 0>(st, p, a.r, b.r);
@@ -1510,11 +1618,11 @@ struct OpBiK2 {
         f = s * inv_of<T, FB>(C, g, v.code, ps);
         return Own{v.code, s, v.r0};
     }
-    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &, const Own &o, const Pos &ps, T fc, T fxp, T fxm,
+    __device__ Out apply(const Geo &g, const Coef<T> &C, Shared &S, const Own &o, const Pos &ps, T fc, T fxp, T fxm,
                          T fyp, T fym, T fzp, T fzm)
     {
         const T d = diag_of<T, FB>(C, g, o.code, ps);
-        const T t = stencil7t<T>(F, C, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
+        const T t = stencil7s(F, S, o.code, fc, fxp, fxm, fyp, fym, fzp, fzm, d);
         ts.add_prod(t, o.s);
         tt.add_prod(t, t);
         r0t.add_prod(o.r0, t);
