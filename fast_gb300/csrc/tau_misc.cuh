@@ -1,6 +1,7 @@
 // MIXED FP64 residual replacement, tau flux reduction, stencil-code build
 // and porosity count.
 #pragma once
+#include <cstring>
 #include <type_traits>
 #include "tau_sweep.cuh"
 
@@ -17,10 +18,99 @@ namespace ft {
 template <typename XT>
 struct XArith;
 
+// Float <-> double conversions with integer instructions, for the FP64
+// replacement: the conversion instructions run on the FP64 pipe, which bounds
+// that kernel, while its integer pipes are mostly idle.  Both are exact for
+// every normal float (the widening copies the bits; the narrowing rounds to
+// nearest even by adding 2^28 - 1 plus the kept mantissa's lowest bit below
+// the cut).  They differ from the conversion instructions only where the
+// solver has no use for the difference: float subnormals become a signed
+// zero, and the narrowing turns a NaN into an infinity of its sign (still
+// non-finite, as the solver's checks ask).  FAST_TAU_INT_CVT=0 uses the
+// conversion instructions.
+#ifndef FAST_TAU_INT_CVT
+#define FAST_TAU_INT_CVT 1
+#endif
+
+__host__ __device__ __forceinline__ uint32_t f_bits(float f)
+{
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+
+__host__ __device__ __forceinline__ double widen_f(float f)
+{
+    const uint32_t u = f_bits(f);
+    const uint32_t sgn = u & 0x80000000u, m = u & 0x7fffffffu;
+    uint32_t hi = sgn | ((m >> 3) + (896u << 20));  // exponent rebias 127 -> 1023
+    uint32_t lo = u << 29;
+    if (m >= 0x7f800000u) hi = sgn | 0x7ff00000u | ((m >> 3) & 0xfffffu);  // infinity, NaN
+    if (m < 0x00800000u) {  // zero, subnormal
+        hi = sgn;
+        lo = 0u;
+    }
+#ifdef __CUDA_ARCH__
+    return __hiloint2double((int)hi, (int)lo);
+#else
+    const uint64_t b = ((uint64_t)hi << 32) | lo;
+    double d;
+    memcpy(&d, &b, 8);
+    return d;
+#endif
+}
+
+__host__ __device__ __forceinline__ float narrow_d(double d)
+{
+#ifdef __CUDA_ARCH__
+    const uint64_t u = (uint64_t)__double_as_longlong(d);
+#else
+    uint64_t u;
+    memcpy(&u, &d, 8);
+#endif
+    const uint32_t sgn = (uint32_t)(u >> 32) & 0x80000000u;
+    const uint32_t e = (uint32_t)(u >> 52) & 0x7ffu;
+    uint64_t v = u & 0x7fffffffffffffffull;
+    v += 0x0fffffffull + ((v >> 29) & 1u);
+    uint32_t r = (uint32_t)(v >> 29) - (896u << 23);  // low word of the rebiased exponent and mantissa
+    if (e > 1150u) r = 0x7f800000u;                  // overflow, infinity, NaN
+    if (e <= 896u) r = 0u;                           // subnormal or zero in FP32
+    float f;
+#ifdef __CUDA_ARCH__
+    f = __uint_as_float(sgn | r);
+#else
+    const uint32_t b = sgn | r;
+    memcpy(&f, &b, 4);
+#endif
+    return f;
+}
+
+__device__ __forceinline__ double to_d(float f)
+{
+#if FAST_TAU_INT_CVT
+    return widen_f(f);
+#else
+    return (double)f;
+#endif
+}
+
+__device__ __forceinline__ float to_f(double d)
+{
+#if FAST_TAU_INT_CVT
+    return narrow_d(d);
+#else
+    return (float)d;
+#endif
+}
+
 template <>
 struct XArith<double> {
     using Tab = Coef<double>;
-    __device__ static double add_f(double x, float e) { return x + (double)e; }
+    __device__ static double add_f(double x, float e) { return x + to_d(e); }
     __device__ static double stencil(const Faces<double> &F, const Tab &C, const Geo &g, uint32_t code,
                                      const Pos &ps, double fc, double fxp, double fxm, double fyp, double fym,
                                      double fzp, double fzm)
@@ -37,10 +127,10 @@ struct XArith<double> {
         const int c = g.coord(ps.x, ps.y, ps.z);
         if (c == 0 || c == g.extent() - 1) {
             const double b = rhs_at<double>(C, g, code, ps.x, ps.y, ps.z);
-            r32 = (float)(b - ax);
-            b32 = (float)b;
+            r32 = to_f(b - ax);
+            b32 = to_f(b);
         } else {
-            r32 = (float)(-ax);
+            r32 = to_f(-ax);
             b32 = 0.f;
         }
     }

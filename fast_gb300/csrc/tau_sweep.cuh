@@ -877,7 +877,7 @@ __device__ __forceinline__ void mixed_bicg_finish(Scalars &sc, double r0r, doubl
 #define FAST_TAU_RPT_CG2 2
 #endif
 #ifndef FAST_TAU_RPT_K2
-#define FAST_TAU_RPT_K2 1
+#define FAST_TAU_RPT_K2 2
 #endif
 
 template <typename TT, typename ST>
