@@ -324,6 +324,10 @@ __host__ __device__ constexpr int sweep_threads()
     return NTHREADS / RowsPerThread<Op>::n;
 }
 
+#ifndef FAST_TAU_FULL_TILE
+#define FAST_TAU_FULL_TILE 1
+#endif
+
 template <class Op, int NSTAGE>
 __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb, bool &ready, int64_t *idle_end)
 {
@@ -468,104 +472,126 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         fm0[r] = fm1[r] = fc0[r] = fc1[r] = fp0[r] = fp1[r] = T(0);
         oc0[r] = oc1[r] = op0[r] = op1[r] = typename Op::Own{};
     }
-    // The operator at plane zs on the thread's points, from the plane
-    // buffer (x and y neighbours; the y neighbour inside the thread's row
-    // pair from its registers) and the field of the planes below (fm) and
-    // above (u0, u1: 0 past the last plane); stores the outputs.
-    auto apply_at = [&](int zs, const T(&u0)[RPT], const T(&u1)[RPT]) {
-        const int bczs = boundary_count_z(g, zs);
-        const T(*P)[PW] = fb[zs % 3];
+    // A tile inside the domain in x and y (most tiles) runs the plane loop
+    // with every point valid as a compile-time fact, which removes the
+    // per-point validity branches; edge tiles test each point.
+    // FAST_TAU_FULL_TILE=0 tests the points of every tile.
+    const bool full = FAST_TAU_FULL_TILE && x0 + TX <= g.nx && y0 + TY <= g.ny;
+    int q = 0;
+    auto march = [&](auto full_c) {
+        constexpr bool FULL = decltype(full_c)::value;
+        auto ok0 = [&](int r) { return FULL || v0[r]; };
+        auto ok1 = [&](int r) { return FULL || v1[r]; };
+        // The operator at plane zs on the thread's points, from the plane
+        // buffer (x and y neighbours; the y neighbour inside the thread's
+        // row pair from its registers) and the field of the planes below
+        // (fm) and above (u0, u1: 0 past the last plane); stores the outputs.
+        auto apply_at = [&](int zs, const T(&u0)[RPT], const T(&u1)[RPT]) {
+            const int bczs = boundary_count_z(g, zs);
+            const T(*P)[PW] = fb[zs % 3];
 #pragma unroll
-        for (int r = 0; r < RPT; ++r) {
-            if (!(v0[r] || v1[r])) continue;
-            const int row = ly0 + r + 1;
-            const Pair<T> left = *reinterpret_cast<const Pair<T> *>(&P[row][2 * lp]);
-            const Pair<T> right = *reinterpret_cast<const Pair<T> *>(&P[row][2 * lp + 4]);
-            T up0, up1, dn0, dn1;
-            if (r + 1 < RPT) {
-                up0 = fc0[r + 1];
-                up1 = fc1[r + 1];
-            } else {
-                const Pair<T> up = *reinterpret_cast<const Pair<T> *>(&P[row + 1][2 * lp + 2]);
-                up0 = up.a;
-                up1 = up.b;
+            for (int r = 0; r < RPT; ++r) {
+                if (!(ok0(r) || ok1(r))) continue;
+                const int row = ly0 + r + 1;
+                const Pair<T> left = *reinterpret_cast<const Pair<T> *>(&P[row][2 * lp]);
+                const Pair<T> right = *reinterpret_cast<const Pair<T> *>(&P[row][2 * lp + 4]);
+                T up0, up1, dn0, dn1;
+                if (r + 1 < RPT) {
+                    up0 = fc0[r + 1];
+                    up1 = fc1[r + 1];
+                } else {
+                    const Pair<T> up = *reinterpret_cast<const Pair<T> *>(&P[row + 1][2 * lp + 2]);
+                    up0 = up.a;
+                    up1 = up.b;
+                }
+                if (r > 0) {
+                    dn0 = fc0[r - 1];
+                    dn1 = fc1[r - 1];
+                } else {
+                    const Pair<T> dn = *reinterpret_cast<const Pair<T> *>(&P[row - 1][2 * lp + 2]);
+                    dn0 = dn.a;
+                    dn1 = dn.b;
+                }
+                const int gy = y0 + ly0 + r;
+                const int64_t i = i_col + (int64_t)r * g.P + plane * zs;
+                typename Op::Out o0{}, o1{};
+                if (ok0(r))
+                    o0 = op.apply(g, C, S, oc0[r], Pos{gx, gy, zs, bc0[r] + bczs}, fc0[r], fc1[r], left.b, up0, dn0,
+                                  u0[r], fm0[r]);
+                if (ok1(r))
+                    o1 = op.apply(g, C, S, oc1[r], Pos{gx + 1, gy, zs, bc1[r] + bczs}, fc1[r], right.a, fc0[r], up1,
+                                  dn1, u1[r], fm1[r]);
+                if (ft_in(J, i, i + 1, plane * g.nz, OOB_SWEEP_STORE)) op.store(i, o0, o1, ok0(r), ok1(r));
             }
-            if (r > 0) {
-                dn0 = fc0[r - 1];
-                dn1 = fc1[r - 1];
-            } else {
-                const Pair<T> dn = *reinterpret_cast<const Pair<T> *>(&P[row - 1][2 * lp + 2]);
-                dn0 = dn.a;
-                dn1 = dn.b;
+        };
+        for (; q < NP; ++q) {
+            const int zq = pa + q;
+            const int st = (qb + q) % NSTAGE;
+            const uint32_t par = (uint32_t)(((qb + q) / NSTAGE) & 1);
+            if (!mbar_wait_bounded<WaitHint<Op>::ns>(smem_u32(&bars[st]), par)) s_err = 1;
+            const unsigned char *stage = sbase + st * SB;
+            const bool out_plane = zq >= z0 && zq < z1;
+            const int bcz = boundary_count_z(g, zq);
+#pragma unroll
+            for (int r = 0; r < RPT; ++r) {
+                const int gy = y0 + ly0 + r;
+                V a, b;
+                Op::load2(stage, Pt{ly0 + r + 1, 2 * lp}, a, b);
+                fp0[r] = T(0);
+                fp1[r] = T(0);
+                if (out_plane) {
+                    if (ok0(r)) op0[r] = op.own(g, C, S, a, Pos{gx, gy, zq, bc0[r] + bcz}, fp0[r]);
+                    if (ok1(r)) op1[r] = op.own(g, C, S, b, Pos{gx + 1, gy, zq, bc1[r] + bcz}, fp1[r]);
+                    *reinterpret_cast<Pair<T> *>(&fb[zq % 3][ly0 + r + 1][2 * lp + 2]) = Pair<T>{fp0[r], fp1[r]};
+                } else {
+                    if (ok0(r)) fp0[r] = op.field(g, C, S, a, Pos{gx, gy, zq, bc0[r] + bcz});
+                    if (ok1(r)) fp1[r] = op.field(g, C, S, b, Pos{gx + 1, gy, zq, bc1[r] + bcz});
+                }
             }
-            const int gy = y0 + ly0 + r;
-            const int64_t i = i_col + (int64_t)r * g.P + plane * zs;
-            typename Op::Out o0{}, o1{};
-            if (v0[r])
-                o0 = op.apply(g, C, S, oc0[r], Pos{gx, gy, zs, bc0[r] + bczs}, fc0[r], fc1[r], left.b, up0, dn0, u0[r],
-                              fm0[r]);
-            if (v1[r])
-                o1 = op.apply(g, C, S, oc1[r], Pos{gx + 1, gy, zs, bc1[r] + bczs}, fc1[r], right.a, fc0[r], up1, dn1,
-                              u1[r], fm1[r]);
-            if (ft_in(J, i, i + 1, plane * g.nz, OOB_SWEEP_STORE)) op.store(i, o0, o1, v0[r], v1[r]);
+            if (out_plane && hkind == 1) {
+                V a, b;
+                HaloLoad<Op>::pair(stage, p_halo, a, b);
+                const T f0 = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
+                const T f1 = h1 ? op.field(g, C, S, b, Pos{hgx + 1, hgy, zq, hbc1 + bcz}) : T(0);
+                *reinterpret_cast<Pair<T> *>(&fb[zq % 3][hrow][hcol]) = Pair<T>{f0, f1};
+            } else if (out_plane && hkind == 2) {
+                V a;
+                Op::load1(stage, p_halo, a);
+                fb[zq % 3][hrow][hcol] = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
+            }
+            __syncthreads();
+            if (s_err) break;
+            // Every thread is done with this stage: refill it with plane
+            // q+NSTAGE.  The last warp issues (the first warps also load the
+            // halo rows).
+            if (tid == kRefillThread && q + NSTAGE < NP) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(q + NSTAGE);
+            }
+            const int zs = zq - 1;
+            if (zs >= z0 && zs < z1 && (FULL || any_v)) apply_at(zs, fp0, fp1);
+#pragma unroll
+            for (int r = 0; r < RPT; ++r) {
+                fm0[r] = fc0[r];
+                fm1[r] = fc1[r];
+                fc0[r] = fp0[r];
+                fc1[r] = fp1[r];
+                oc0[r] = op0[r];
+                oc1[r] = op1[r];
+            }
+        }
+        // The last plane of the volume has no z+1 neighbour: apply it here.
+        if (!s_err && pb == z1 - 1 && (FULL || any_v)) {
+            T zero[RPT];
+#pragma unroll
+            for (int r = 0; r < RPT; ++r) zero[r] = T(0);
+            apply_at(z1 - 1, zero, zero);
         }
     };
-    int q = 0;
-    for (; q < NP; ++q) {
-        const int zq = pa + q;
-        const int st = (qb + q) % NSTAGE;
-        const uint32_t par = (uint32_t)(((qb + q) / NSTAGE) & 1);
-        if (!mbar_wait_bounded<WaitHint<Op>::ns>(smem_u32(&bars[st]), par)) s_err = 1;
-        const unsigned char *stage = sbase + st * SB;
-        const bool out_plane = zq >= z0 && zq < z1;
-        const int bcz = boundary_count_z(g, zq);
-#pragma unroll
-        for (int r = 0; r < RPT; ++r) {
-            const int gy = y0 + ly0 + r;
-            V a, b;
-            Op::load2(stage, Pt{ly0 + r + 1, 2 * lp}, a, b);
-            fp0[r] = T(0);
-            fp1[r] = T(0);
-            if (out_plane) {
-                if (v0[r]) op0[r] = op.own(g, C, S, a, Pos{gx, gy, zq, bc0[r] + bcz}, fp0[r]);
-                if (v1[r]) op1[r] = op.own(g, C, S, b, Pos{gx + 1, gy, zq, bc1[r] + bcz}, fp1[r]);
-                *reinterpret_cast<Pair<T> *>(&fb[zq % 3][ly0 + r + 1][2 * lp + 2]) = Pair<T>{fp0[r], fp1[r]};
-            } else {
-                if (v0[r]) fp0[r] = op.field(g, C, S, a, Pos{gx, gy, zq, bc0[r] + bcz});
-                if (v1[r]) fp1[r] = op.field(g, C, S, b, Pos{gx + 1, gy, zq, bc1[r] + bcz});
-            }
-        }
-        if (out_plane && hkind == 1) {
-            V a, b;
-            HaloLoad<Op>::pair(stage, p_halo, a, b);
-            const T f0 = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
-            const T f1 = h1 ? op.field(g, C, S, b, Pos{hgx + 1, hgy, zq, hbc1 + bcz}) : T(0);
-            *reinterpret_cast<Pair<T> *>(&fb[zq % 3][hrow][hcol]) = Pair<T>{f0, f1};
-        } else if (out_plane && hkind == 2) {
-            V a;
-            Op::load1(stage, p_halo, a);
-            fb[zq % 3][hrow][hcol] = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
-        }
-        __syncthreads();
-        if (s_err) break;
-        // Every thread is done with this stage: refill it with plane q+NSTAGE.
-        // The last warp issues (the first warps also load the halo rows).
-        if (tid == kRefillThread && q + NSTAGE < NP) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(q + NSTAGE);
-        }
-        const int zs = zq - 1;
-        if (zs >= z0 && zs < z1 && any_v) apply_at(zs, fp0, fp1);
-#pragma unroll
-        for (int r = 0; r < RPT; ++r) {
-            fm0[r] = fc0[r];
-            fm1[r] = fc1[r];
-            fc0[r] = fp0[r];
-            fc1[r] = fp1[r];
-            oc0[r] = op0[r];
-            oc1[r] = op1[r];
-        }
-    }
+    if (full)
+        march(std::true_type{});
+    else
+        march(std::false_type{});
 
     if (s_err) {
         // Tile loads did not arrive in time.  Wait (bounded) for the copies
@@ -579,13 +605,6 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         return SWEEP_FAULT;
     }
     qb += NP;
-    // The last plane of the volume has no z+1 neighbour: apply it here.
-    if (pb == z1 - 1 && any_v) {
-        T zero[RPT];
-#pragma unroll
-        for (int r = 0; r < RPT; ++r) zero[r] = T(0);
-        apply_at(z1 - 1, zero, zero);
-    }
 
     using RT = typename RedType<Op>::type;
     RT v[NV];
