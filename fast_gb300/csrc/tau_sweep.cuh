@@ -488,7 +488,7 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         // (fm) and above (u0, u1: 0 past the last plane); stores the outputs.
         auto apply_at = [&](int zs, const T(&u0)[RPT], const T(&u1)[RPT]) {
             const int bczs = boundary_count_z(g, zs);
-            const T(*P)[PW] = fb[zs % 3];
+            const T(*P)[PW] = fb[(unsigned)zs % 3u];
 #pragma unroll
             for (int r = 0; r < RPT; ++r) {
                 if (!(ok0(r) || ok1(r))) continue;
@@ -526,8 +526,10 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
         };
         for (; q < NP; ++q) {
             const int zq = pa + q;
-            const int st = (qb + q) % NSTAGE;
-            const uint32_t par = (uint32_t)(((qb + q) / NSTAGE) & 1);
+            // ring slot and phase (plane counts are never negative)
+            const int st = (int)((unsigned)(qb + q) % (unsigned)NSTAGE);
+            const uint32_t par = ((unsigned)(qb + q) / (unsigned)NSTAGE) & 1u;
+            const unsigned zb = (unsigned)zq % 3u;  // plane-buffer slot
             if (!mbar_wait_bounded<WaitHint<Op>::ns>(smem_u32(&bars[st]), par)) s_err = 1;
             const unsigned char *stage = sbase + st * SB;
             const bool out_plane = zq >= z0 && zq < z1;
@@ -542,7 +544,7 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
                 if (out_plane) {
                     if (ok0(r)) op0[r] = op.own(g, C, S, a, Pos{gx, gy, zq, bc0[r] + bcz}, fp0[r]);
                     if (ok1(r)) op1[r] = op.own(g, C, S, b, Pos{gx + 1, gy, zq, bc1[r] + bcz}, fp1[r]);
-                    *reinterpret_cast<Pair<T> *>(&fb[zq % 3][ly0 + r + 1][2 * lp + 2]) = Pair<T>{fp0[r], fp1[r]};
+                    *reinterpret_cast<Pair<T> *>(&fb[zb][ly0 + r + 1][2 * lp + 2]) = Pair<T>{fp0[r], fp1[r]};
                 } else {
                     if (ok0(r)) fp0[r] = op.field(g, C, S, a, Pos{gx, gy, zq, bc0[r] + bcz});
                     if (ok1(r)) fp1[r] = op.field(g, C, S, b, Pos{gx + 1, gy, zq, bc1[r] + bcz});
@@ -553,11 +555,11 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
                 HaloLoad<Op>::pair(stage, p_halo, a, b);
                 const T f0 = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
                 const T f1 = h1 ? op.field(g, C, S, b, Pos{hgx + 1, hgy, zq, hbc1 + bcz}) : T(0);
-                *reinterpret_cast<Pair<T> *>(&fb[zq % 3][hrow][hcol]) = Pair<T>{f0, f1};
+                *reinterpret_cast<Pair<T> *>(&fb[zb][hrow][hcol]) = Pair<T>{f0, f1};
             } else if (out_plane && hkind == 2) {
                 V a;
                 Op::load1(stage, p_halo, a);
-                fb[zq % 3][hrow][hcol] = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
+                fb[zb][hrow][hcol] = h0 ? op.field(g, C, S, a, Pos{hgx, hgy, zq, hbc0 + bcz}) : T(0);
             }
             __syncthreads();
             if (s_err) break;
