@@ -35,19 +35,52 @@ constexpr int kBlocksK1 = 3;
 #ifndef FAST_TAU_MINB_R2
 #define FAST_TAU_MINB_R2 0
 #endif
-// A sweep with two rows per thread runs half-size blocks, which the fixed
-// shared memory of a block (plane buffers, tables) already limits to few
-// per SM: its stage ring is shorter, and FAST_TAU_MINB_R2 > 0 bounds its
-// registers to fit that many blocks per SM.
+#ifndef FAST_TAU_STAGES_CG1
+#define FAST_TAU_STAGES_CG1 3
+#endif
+#ifndef FAST_TAU_MINB_CG2
+#define FAST_TAU_MINB_CG2 7
+#endif
+#ifndef FAST_TAU_MINB_K2
+#define FAST_TAU_MINB_K2 7
+#endif
+// Ring depth and register bound of a sweep.  A sweep with two rows per
+// thread runs half-size blocks, which the fixed shared memory of a block
+// (plane buffers, tables) already limits to few per SM: its stage ring is
+// shorter (FAST_TAU_STAGES_R2), and a minimum of blocks per SM > 0 bounds
+// its registers.  Measured per sweep (256^3 and 512^3, MIXED): PCG step 1
+// with a 3-stage ring (six blocks per SM either way), PCG step 2 and
+// BiCGSTAB step 2 with 2 stages and a bound of 72 registers.
+template <class Op>
+struct SweepShape {
+    static constexpr int stages = RowsPerThread<Op>::n == 2 ? FAST_TAU_STAGES_R2 : kStages;
+    static constexpr int minb = RowsPerThread<Op>::n == 2 ? FAST_TAU_MINB_R2 : 0;
+};
+template <>
+struct SweepShape<OpCG1<float, double>> {
+    static constexpr int stages = RowsPerThread<OpCG1<float, double>>::n == 2 ? FAST_TAU_STAGES_CG1 : kStages;
+    static constexpr int minb = 0;
+};
+template <>
+struct SweepShape<OpCG2<float, double>> {
+    static constexpr int stages = RowsPerThread<OpCG2<float, double>>::n == 2 ? FAST_TAU_STAGES_R2 : kStages;
+    static constexpr int minb = RowsPerThread<OpCG2<float, double>>::n == 2 ? FAST_TAU_MINB_CG2 : 0;
+};
+template <>
+struct SweepShape<OpBiK2> {
+    static constexpr int stages = RowsPerThread<OpBiK2>::n == 2 ? FAST_TAU_STAGES_R2 : kStages;
+    static constexpr int minb = RowsPerThread<OpBiK2>::n == 2 ? FAST_TAU_MINB_K2 : 0;
+};
+
 template <class Op>
 constexpr int stages_of()
 {
-    return RowsPerThread<Op>::n == 2 ? FAST_TAU_STAGES_R2 : kStages;
+    return SweepShape<Op>::stages;
 }
 template <class Op>
 constexpr int min_blocks_of()
 {
-    return RowsPerThread<Op>::n == 2 ? FAST_TAU_MINB_R2 : 0;
+    return SweepShape<Op>::minb;
 }
 
 template <class Op, int NS = stages_of<Op>()>
