@@ -39,7 +39,7 @@ constexpr int kBlocksK1 = 3;
 #define FAST_TAU_STAGES_CG1 3
 #endif
 #ifndef FAST_TAU_MINB_CG2
-#define FAST_TAU_MINB_CG2 7
+#define FAST_TAU_MINB_CG2 0
 #endif
 #ifndef FAST_TAU_MINB_K2
 #define FAST_TAU_MINB_K2 7
@@ -48,9 +48,10 @@ constexpr int kBlocksK1 = 3;
 // thread runs half-size blocks, which the fixed shared memory of a block
 // (plane buffers, tables) already limits to few per SM: its stage ring is
 // shorter (FAST_TAU_STAGES_R2), and a minimum of blocks per SM > 0 bounds
-// its registers.  Measured per sweep (256^3 and 512^3, MIXED): PCG step 1
-// with a 3-stage ring (six blocks per SM either way), PCG step 2 and
-// BiCGSTAB step 2 with 2 stages and a bound of 72 registers.
+// its registers.  Measured per sweep (MIXED): PCG step 1 with a 3-stage
+// ring (six blocks per SM either way), PCG step 2 with 2 stages (a bound of
+// 72 registers was faster at 256^3 but slower at the 1024^3 depth of 256
+// planes), BiCGSTAB step 2 with 2 stages and the 72-register bound.
 template <class Op>
 struct SweepShape {
     static constexpr int stages = RowsPerThread<Op>::n == 2 ? FAST_TAU_STAGES_R2 : kStages;
