@@ -453,11 +453,11 @@ C_RESULT_BYTES = 40  # sizeof(fast_tau_result)
 # --set full capture of a one-direction launch of the same volume
 # (profiles/), scaled by 3 to the three right-hand sides a bench launch
 # processes (traffic grows with the voxels).
-NCU_TRAFFIC = {"bi1": 3 * 668.9e6, "bi2": 3 * 276.1e6}
+NCU_TRAFFIC = {"bi1": 3 * 672.3e6, "bi2": 3 * 276.2e6}
 # DRAM bytes per voxel-iteration of the two PCG sweeps at the large-volume
 # slab depth (ncu dram__bytes_read.sum + dram__bytes_write.sum of OpCG1 and
-# OpCG2 on the 512^3 spheres at 256 planes per block: 13.02 + 20.77).
-C5_DRAM_BYTES_PER_VOXEL_ITER = 33.79
+# OpCG2 on the 512^3 spheres at 256 planes per block: 13.04 + 21.48).
+C5_DRAM_BYTES_PER_VOXEL_ITER = 34.52
 
 
 # ---------------------------------------------------------------------------
