@@ -3,8 +3,9 @@
 //
 // One thread block owns a TX x TY column tile of one right-hand side and
 // marches the planes z0..z1-1 of its slab; each thread owns two neighbouring
-// x columns.  The state vectors an operation reads arrive through TMA: for
-// every plane, thread 0 issues one cp.async.bulk.tensor tile load per vector
+// x columns of one row (or of two rows, for the operations that name
+// RPT = 2).  The state vectors an operation reads arrive through TMA: for
+// every plane, one thread issues one cp.async.bulk.tensor tile load per vector
 // (the tile plus a one-voxel x/y halo, widened in x to the 16-byte TMA
 // alignment) into a ring of NSTAGE shared-memory stages, each completed on
 // its own mbarrier, so NSTAGE-1 planes of every vector are in flight while

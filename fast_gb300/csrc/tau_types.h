@@ -7,7 +7,9 @@ namespace ft {
 
 // Tile of one thread block: TX x TY columns marching over ZC planes in z.
 // Each thread owns two neighbouring x columns (LANES), so a row of TX
-// voxels is TPR threads; a block is always 256 threads (TX * TY = 512).
+// voxels is TPR threads; NTHREADS = 256 threads cover the TX * TY = 512
+// columns with one row each (a sweep with two rows per thread runs
+// NTHREADS / 2).
 #ifndef FAST_TAU_TX
 #define FAST_TAU_TX 64
 #endif
