@@ -409,7 +409,8 @@ __device__ __forceinline__ int sweep_body(const Launch &L, int64_t blk, int &qb,
     }
     ready = true;
     __syncthreads();
-    // Tile loads of plane pa+q into ring slot (qb + q) % NSTAGE (thread 0 only).
+    // Tile loads of plane pa+q into ring slot (qb + q) % NSTAGE (one thread:
+    // thread 0 for the first NSTAGE planes, the refill thread after).
     auto issue = [&](int q) {
 #if FAST_TAU_TEST_HOOKS
         if (q == 1 && local == 0 && atomicExch(&J.sc->test_withhold, 0) != 0) return;
