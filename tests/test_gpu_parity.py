@@ -193,6 +193,29 @@ def test_edge_shapes(gpu, oracle, shape):
                 assert rel(tau, ref["tau"]) <= 1e-7, (shape, d, solver, tau, ref)
 
 
+@pytest.mark.parametrize("shape", [(1, 5, 1), (3, 1, 1), (2, 3, 1), (5, 3, 70), (7, 17, 9), (33, 9, 65),
+                                   (4, 12, 130)])
+def test_mixed_edge_shapes(gpu, oracle, shape):
+    """MIXED (the FP32 sweeps with two rows per thread, the full-tile and the
+    edge-tile plane loops, the FP64 replacement) on one-voxel axes, rows and
+    columns that fill no tile, and tiles whose second thread row lies past
+    the volume, in every direction: within 1e-6 of the oracle's FP64 CG at
+    tol 1e-11, solved to tol 1e-10."""
+    rng = np.random.default_rng(7 + sum(shape))
+    mask = ((rng.random(shape) < 0.35) * 255).astype(np.uint8)
+    for d in range(6):
+        ref = oracle.get_tortuosity(mask, dir=d, solver=1, tol=1e-11)
+        if ref["status"] != 0:
+            continue
+        for solver in (ft.DSOLVER_CG, ft.DSOLVER_BICGSTAB):
+            p = ft.TortuosityParams(dir=ft.Dir(d), tolerance=1e-10, precision=ft.Precision.MIXED)
+            tau = ft.get_tortuosity(mask, p, solver)
+            if ref["tau"] == 0.0:
+                assert tau == 0.0, (shape, d, solver, tau)
+            else:
+                assert rel(tau, ref["tau"]) <= 1e-6, (shape, d, solver, tau, ref)
+
+
 def test_concentration_output(gpu, oracle):
     mask = _vol((16, 18, 20), seed=4)
     p = ft.TortuosityParams(dir=ft.Dir.Z_NEG, tolerance=1e-11)
